@@ -1,0 +1,140 @@
+// Arithmetic policies for one lifting update
+//   g[k] = c0 * g[k - s] + c1 * g[k] + c2 * g[k + s]
+// (paliwa/paliwa_transform.hpp:46-49). Every policy keeps the reference's
+// evaluation order ((c0*lo + c1*me) + c2*up).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace pgb {
+
+struct Coeffs {
+  double c0, c1, c2;
+};
+
+// ---------------------------------------------------------------------------
+// Plain IEEE arithmetic in T (double or float).
+//
+// ExactProducts: the host has checked that every coefficient is 0 or a power
+// of two, so each product c*x is exact. Then
+//   fma(c0, lo, c1*me) == round(round(c0*lo) + round(c1*me))
+// and the fused form is bit-identical to the reference's separately rounded
+// expression while issuing two FMAs per update (one more multiply only when
+// c1 != 1). Otherwise every product and sum is rounded separately with the
+// _rn intrinsics, which the compiler never contracts.
+template <typename T, bool ExactProducts> struct Plain {
+  using V = T;
+  using Store = T;
+  static __device__ __forceinline__ V load(Store x) { return x; }
+  static __device__ __forceinline__ Store store(V x) { return x; }
+
+  static constexpr bool kHasFp64Mode = false;
+
+  // C1: the middle coefficient is exactly 1 (skips one multiply).
+  // F64: unused (plain arithmetic has a single precision).
+  template <bool C1, bool F64>
+  static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
+                                             V up) {
+    if constexpr (ExactProducts) {
+      V t = C1 ? me : mul(T(c.c1), me);
+      t = fma(T(c.c0), lo, t);
+      return fma(T(c.c2), up, t);
+    } else {
+      V t = add(mul(T(c.c0), lo), C1 ? me : mul(T(c.c1), me));
+      return add(t, mul(T(c.c2), up));
+    }
+  }
+
+ private:
+  static __device__ __forceinline__ double mul(double a, double b) {
+    return __dmul_rn(a, b);
+  }
+  static __device__ __forceinline__ float mul(float a, float b) {
+    return __fmul_rn(a, b);
+  }
+  static __device__ __forceinline__ double add(double a, double b) {
+    return __dadd_rn(a, b);
+  }
+  static __device__ __forceinline__ float add(float a, float b) {
+    return __fadd_rn(a, b);
+  }
+  static __device__ __forceinline__ double fma(double a, double b, double c) {
+    return __fma_rn(a, b, c);
+  }
+  static __device__ __forceinline__ float fma(float a, float b, float c) {
+    return __fmaf_rn(a, b, c);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// FP32 storage with compensated (double-float) arithmetic.
+//
+// A value in registers is an unevaluated pair h + l of floats. Loads start
+// with l = 0. Each update evaluates c0*lo + c1*me + c2*up with error-free
+// transformations (FMA-based TwoProd, Knuth TwoSum), so rounding errors do not
+// accumulate along the level chain; the pair is rounded to one float only
+// when it is stored, i.e. once per dimension. The coarsest levels (at most a
+// few points per pencil) are evaluated in FP64, as the mass-conservation
+// property of those steps is the most sensitive to rounding.
+struct DF {
+  float h, l;
+};
+
+__device__ __forceinline__ DF two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return {s, e};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  DF s = two_sum(a.h, b.h);
+  float e = __fadd_rn(s.l, __fadd_rn(a.l, b.l));
+  return fast_two_sum(s.h, e);
+}
+// c * a for a float coefficient c: TwoProd on the high part plus the low part.
+__device__ __forceinline__ DF df_scale(float c, DF a) {
+  float p = __fmul_rn(c, a.h);
+  float e = __fmaf_rn(c, a.h, -p);
+  e = __fmaf_rn(c, a.l, e);
+  return {p, e};
+}
+
+struct Compensated {
+  using V = DF;
+  using Store = float;
+  static __device__ __forceinline__ V load(Store x) { return {x, 0.0f}; }
+  static __device__ __forceinline__ Store store(V x) {
+    return __fadd_rn(x.h, x.l);
+  }
+  static constexpr bool kHasFp64Mode = true;
+
+  static __device__ __forceinline__ double to_double(DF x) {
+    return double(x.h) + double(x.l);
+  }
+  static __device__ __forceinline__ DF from_double(double d) {
+    float h = __double2float_rn(d);
+    return {h, __double2float_rn(d - double(h))};
+  }
+  template <bool C1, bool F64>
+  static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
+                                             V up) {
+    if constexpr (F64) {
+      double const m = to_double(me);
+      double t = C1 ? m : __dmul_rn(c.c1, m);
+      t = __fma_rn(c.c0, to_double(lo), t);
+      return from_double(__fma_rn(c.c2, to_double(up), t));
+    } else {
+      DF p0 = df_scale(float(c.c0), lo);
+      DF p1 = C1 ? me : df_scale(float(c.c1), me);
+      DF p2 = df_scale(float(c.c2), up);
+      return df_add(df_add(p0, p1), p2);
+    }
+  }
+};
+
+} // namespace pgb

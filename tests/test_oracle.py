@@ -1,0 +1,114 @@
+"""The CPU oracle against the reference's own tests (no GPU needed)."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "plan_multipass.npz")
+
+
+def golden_filters(passes, mask):
+    # test/test_paliwa_plan.cpp:121-125
+    return [((1 if mask & (1 << p) else 0),
+             (0.0, 1.0, 0.25) if p % 2 else (-0.5, 1.0, 0.125))
+            for p in range(passes)]
+
+
+def test_oracle_matches_reference_test_loop(oracle_mod):
+    """test/test_paliwa_plan.cpp:114-163: the transform of the level-4 grid
+    inside maximum level 6 equals the reference's own 1D periodic loop."""
+    g = np.load(GOLDEN)
+    inp, cases, out = g["input"], g["cases"], g["output"]
+    for (passes, mask, order), expected in zip(cases, out):
+        levels = [4, 3, 2, 1] if order == 0 else [1, 2, 3, 4]
+        grid = inp[::4].copy()  # uids 0, 4, ..., 60: the level-4 grid
+        for mode in (0, 1):
+            got = oracle_mod.transform_in(grid.copy(), [4], [6], 0, levels,
+                                          golden_filters(passes, mask), mode)
+            assert np.array_equal(got, expected[::4]), (passes, mask, order)
+        # points off the level-4 lattice are never written by the loop
+        others = np.ones(64, bool)
+        others[::4] = False
+        assert np.array_equal(expected[others], inp[others])
+
+
+def seeded_grid(shape, seed):
+    rng = np.random.default_rng(seed)
+    return rng.random(shape)
+
+
+@pytest.mark.parametrize("lmin", [(0, 0), (0, 1), (0, 3), (1, 0), (1, 1),
+                                  (1, 3), (3, 0), (3, 1), (3, 3)])
+def test_hat_stays_same_2d(oracle_mod, lmin):
+    """test/test_paliwa_transform.cpp:17-79 (level (3,3) in (4,4)): points of
+    the lmin grid keep their values (1e-14), every other point changes, and
+    dehierarchize undoes hierarchize (1e-13). The reference draws its input
+    from Kokkos' XorShift64 pool (seed 12345), which is not reproducible
+    without Kokkos; the input here has the same form (1 + ix + iy) * (1 + u)
+    with u from a seeded numpy generator."""
+    level, lmax = (3, 3), (4, 4)
+    ix = np.arange(8)[:, None] * 2
+    iy = np.arange(8)[None, :] * 2
+    x = (1 + ix + iy) * (1 + seeded_grid((8, 8), 12345))
+    y = x.copy()
+    oracle_mod.hierarchize(y, level, lmin, lmax, "hat")
+    sx, sy = 1 << (level[0] - lmin[0]), 1 << (level[1] - lmin[1])
+    on_lmin = np.zeros((8, 8), bool)
+    on_lmin[::sx, ::sy] = True
+    assert np.all(np.abs(y[on_lmin] - x[on_lmin]) <= 1e-14)
+    assert np.all(y[~on_lmin] != x[~on_lmin])
+    oracle_mod.dehierarchize(y, level, lmin, lmax, "hat")
+    assert np.max(np.abs(y - x)) <= 1e-13
+
+
+@pytest.mark.parametrize("wavelet", ["biorthogonal", "fullweighting"])
+def test_mass_conservation_2d(oracle_mod, wavelet):
+    """test/test_paliwa_transform.cpp:81-143: after hierarchization the sum
+    over the lmin grid equals mean * count to 1e-13 (every wavelet but hat)."""
+    level, lmax = (3, 3), (4, 4)
+    ix = np.arange(8)[:, None] * 2
+    iy = np.arange(8)[None, :] * 2
+    for lmin in [(a, b) for a in (0, 1, 3) for b in (0, 1, 3)]:
+        x = (1 + ix + iy) * (1 + seeded_grid((8, 8), 12345))
+        avg = x.sum() / x.size
+        y = oracle_mod.hierarchize(x.copy(), level, lmin, lmax, wavelet)
+        sx, sy = 1 << (level[0] - lmin[0]), 1 << (level[1] - lmin[1])
+        sub = y[::sx, ::sy]
+        assert abs(sub.sum() - avg * sub.size) <= 1e-13
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("wavelet", ["hat", "biorthogonal", "fullweighting"])
+def test_direct_and_packed_poles_agree(oracle_mod, dtype, wavelet):
+    """Both reference execution modes (PoleExecution::Direct and
+    PackedPoles, paliwa/paliwa_transform.hpp:21) compute identical values."""
+    for level, lmin in [((5,), (0,)), ((3, 4), (1, 0)), ((2, 3, 4), (0, 1, 2)),
+                        ((4, 1, 3, 2), (2, 0, 0, 1))]:
+        lmax = tuple(l + 1 for l in level)
+        x = seeded_grid([1 << l for l in level], 7).astype(dtype)
+        for fwd in (True, False):
+            a = oracle_mod.hierarchize(x.copy(), level, lmin, lmax, wavelet,
+                                       forward=fwd, mode=0)
+            b = oracle_mod.hierarchize(x.copy(), level, lmin, lmax, wavelet,
+                                       forward=fwd, mode=1)
+            assert np.array_equal(a, b)
+
+
+def test_round_trip_all_wavelets(oracle_mod):
+    for wavelet in ("hat", "biorthogonal", "fullweighting"):
+        level, lmin, lmax = (6, 5, 4), (0, 2, 1), (7, 5, 6)
+        x = seeded_grid([64, 32, 16], 3)
+        y = oracle_mod.hierarchize(x.copy(), level, lmin, lmax, wavelet)
+        oracle_mod.dehierarchize(y, level, lmin, lmax, wavelet)
+        assert np.max(np.abs(y - x)) <= 1e-13
+
+
+def test_oracle_errors(oracle_mod):
+    x = np.zeros((4, 4))
+    with pytest.raises(KeyError):
+        oracle_mod.hierarchize(x, (2, 2), (0, 0), (2, 2), "db4")
+    with pytest.raises(ValueError):
+        oracle_mod.hierarchize(x, (2, 2), (3, 0), (2, 2), "hat")
+    with pytest.raises(RuntimeError):  # paliwa_transform.hpp:239-240
+        oracle_mod.transform_in(x, (2, 2), (2, 2), 0, [2], [(2, (0, 1, 0))])

@@ -1,0 +1,179 @@
+"""GPU parity: the sm_103a kernels against the CPU oracle, through the C ABI.
+
+FP64 and plain FP32 are bit-identical to the oracle (the reference's
+arithmetic with its evaluation order). FP32-compensated is checked against
+the FP64 oracle with a normwise tolerance of 1e-6 (max |err| / max |ref|).
+"""
+import numpy as np
+import pytest
+
+import paliwa_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+WAVELETS = ["hat", "biorthogonal", "fullweighting"]
+F32C_TOL = 1e-6
+
+
+def torch_dev(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def gpu_transform(x, level, lmin, lmax, wavelet, forward, compensated=False):
+    t = torch_dev(x)
+    fn = pg.hierarchize if forward else pg.dehierarchize
+    fn(t, level, lmin, lmax, wavelet, compensated=compensated)
+    return host(t)
+
+
+def random_input(level, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-1.0, 1.0, [1 << l for l in level])
+
+
+SHAPES = [
+    ((1,), (0,)), ((2,), (0,)), ((5,), (1,)), ((9,), (0,)), ((12,), (3,)),
+    ((13,), (0,)),
+    ((6, 6), (0, 0)), ((3, 3), (1, 3)), ((4, 9), (2, 0)), ((10, 2), (0, 1)),
+    ((1, 12), (0, 5)),
+    ((5, 4, 3), (0, 1, 2)), ((2, 7, 5), (1, 0, 0)), ((3, 1, 8), (0, 0, 0)),
+    ((2, 2, 3, 4), (1, 0, 2, 0)), ((3, 2, 1, 2, 1, 2), (0, 0, 0, 1, 0, 0)),
+]
+
+
+@pytest.mark.parametrize("wavelet", WAVELETS)
+@pytest.mark.parametrize("level,lmin", SHAPES)
+def test_f64_bit_exact(level, lmin, wavelet):
+    lmax = tuple(l + 2 for l in level)
+    x = random_input(level, sum(level) + 11)
+    for forward in (True, False):
+        want = import_oracle().hierarchize(x.copy(), level, lmin, lmax,
+                                           wavelet, forward=forward)
+        got = gpu_transform(x, level, lmin, lmax, wavelet, forward)
+        assert np.array_equal(got, want), (level, lmin, wavelet, forward)
+
+
+@pytest.mark.parametrize("wavelet", WAVELETS)
+@pytest.mark.parametrize("level,lmin", SHAPES[::2])
+def test_f32_plain_bit_exact(level, lmin, wavelet):
+    lmax = tuple(level)
+    x = random_input(level, 5).astype(np.float32)
+    for forward in (True, False):
+        want = import_oracle().hierarchize(x.copy(), level, lmin, lmax,
+                                           wavelet, forward=forward)
+        got = gpu_transform(x, level, lmin, lmax, wavelet, forward)
+        assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("wavelet", WAVELETS)
+@pytest.mark.parametrize("level,lmin", SHAPES)
+def test_f32_compensated_error(level, lmin, wavelet):
+    lmax = tuple(level)
+    x = random_input(level, 9)
+    for forward in (True, False):
+        want = import_oracle().hierarchize(x.copy(), level, lmin, lmax,
+                                           wavelet, forward=forward)
+        got = gpu_transform(x.astype(np.float32), level, lmin, lmax, wavelet,
+                            forward, compensated=True).astype(np.float64)
+        scale = max(np.max(np.abs(want)), 1e-300)
+        err = np.max(np.abs(got - want)) / scale
+        assert err <= F32C_TOL, (level, wavelet, forward, err)
+
+
+LONG = [((14,), (0,)), ((15,), (2,)), ((17,), (0,)), ((16, 1), (3, 0)),
+        ((2, 15), (0, 0)), ((14, 2), (0, 1)), ((1, 1, 1, 17), (1, 1, 1, 1))]
+
+
+@pytest.mark.parametrize("wavelet", WAVELETS)
+@pytest.mark.parametrize("level,lmin", LONG)
+def test_long_pencils_bit_exact(level, lmin, wavelet):
+    """Pencils longer than one CTA holds: fine levels on windows with halos,
+    coarse levels on the strided sub-lattice."""
+    lmax = tuple(level)
+    x = random_input(level, 21)
+    for forward in (True, False):
+        want = import_oracle().hierarchize(x.copy(), level, lmin, lmax,
+                                           wavelet, forward=forward)
+        got = gpu_transform(x, level, lmin, lmax, wavelet, forward)
+        assert np.array_equal(got, want), (level, wavelet, forward)
+
+
+def golden_filters(passes, mask):
+    return [((1 if mask & (1 << p) else 0),
+             (0.0, 1.0, 0.25) if p % 2 else (-0.5, 1.0, 0.125))
+            for p in range(passes)]
+
+
+def test_transform_in_reference_loop_golden():
+    """transform_in with the generic filter lists of
+    test/test_paliwa_plan.cpp:114-163 matches the committed golden vectors of
+    the reference's own 1D loop, bit for bit."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden",
+                             "plan_multipass.npz"))
+    for (passes, mask, order), expected in zip(g["cases"], g["output"]):
+        levels = [4, 3, 2, 1] if order == 0 else [1, 2, 3, 4]
+        t = torch_dev(g["input"][::4].copy())
+        pg.transform_in(t, 0, (4,), (6,), levels, golden_filters(passes, mask))
+        assert np.array_equal(host(t), expected[::4]), (passes, mask, order)
+
+
+@pytest.mark.parametrize("level,dim", [((6, 5), 0), ((6, 5), 1), ((3, 14), 1),
+                                       ((15, 2), 0)])
+def test_transform_in_general_coefficients(level, dim):
+    """Coefficients that are not powers of two use separately rounded
+    products and sums: still bit-identical to the oracle. Levels in any
+    order, repeated levels included."""
+    filters = [(1, (-0.3, 1.1, 0.7)), (0, (0.2, 0.9, -0.15)),
+               (1, (0.1, 1.0, 0.1))]
+    lev = level[dim]
+    levels = [lev, 1, 2, lev - 1, 2]
+    lmax = tuple(l + 1 for l in level)
+    x = random_input(level, 4)
+    want = import_oracle().transform_in(x.copy(), level, lmax, dim, levels,
+                                        filters)
+    t = torch_dev(x)
+    pg.transform_in(t, dim, level, lmax, levels, filters)
+    assert np.array_equal(host(t), want)
+
+
+def test_per_dimension_calls_compose():
+    level, lmin, lmax = (4, 5, 3), (1, 0, 2), (4, 5, 3)
+    x = random_input(level, 8)
+    want = import_oracle().hierarchize(x.copy(), level, lmin, lmax,
+                                       "biorthogonal")
+    t = torch_dev(x)
+    for d in range(3):
+        assert pg.hierarchize_in(t, d, level, lmin, lmax, "biorthogonal")
+    assert np.array_equal(host(t), want)
+    for d in range(3):
+        pg.dehierarchize_in(t, d, level, lmin, lmax, "biorthogonal")
+    assert np.max(np.abs(host(t) - x)) <= 1e-13
+
+
+def test_errors_on_gpu():
+    import torch
+    t = torch.zeros(16, dtype=torch.float64, device="cuda")
+    with pytest.raises(pg.PaliwaError, match="Filter offset not supported"):
+        pg.transform_in(t, 0, (4,), (4,), [4], [(2, (0.0, 1.0, 0.0))])
+    with pytest.raises(pg.OutOfRange):
+        pg.hierarchize(t, (4,), (0,), (4,), "nope")
+    with pytest.raises(pg.InvalidArgument):
+        pg.hierarchize(t, (4,), (5,), (4,), "hat")
+    with pytest.raises(pg.InvalidArgument):
+        pg.hierarchize(t, (3,), (0,), (4,), "hat")  # wrong size
+    with pytest.raises(pg.InvalidArgument):
+        pg.hierarchize(t.cpu(), (4,), (0,), (4,), "hat")
+
+
+def import_oracle():
+    import oracle
+    oracle.build()
+    return oracle

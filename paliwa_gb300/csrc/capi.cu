@@ -300,7 +300,8 @@ std::vector<int> level_shifts(int64_t lev, int64_t lmin, bool forward) {
   // dehierarchize_in: lmin+1 .. lev (:392-394). shift = lev - l.
   for (int64_t l = lmin + 1; l <= lev; ++l)
     sh.push_back(static_cast<int>(lev - l));
-  if (!forward) std::reverse(sh.begin(), sh.end());
+  // sh now follows increasing levels (the inverse order).
+  if (forward) std::reverse(sh.begin(), sh.end());
   return sh;
 }
 

@@ -115,6 +115,76 @@ int paliwa_gb_dehierarchize(void *grid, int dtype, int ndim,
                             const int64_t *maximum_level, int wavelet,
                             void *stream);
 
+/* ------------------------------------------------------------------------
+ * Batched transforms of many component grids.
+ *
+ * Replaces the per-grid loop of the reference's combination-technique driver,
+ * paliwa::hierarchize(grid_i, level_i, lmin, lmax, wavelet, instances[i % n])
+ * (test/test_paliwa_combination_technique.cpp:164-174), and its
+ * dehierarchize counterpart. grid_ptrs[i] is the device address of grid i
+ * (dense row-major, 2^sum(levels[i*ndim .. i*ndim+ndim-1]) values of dtype);
+ * the pointers are bound at creation. Each direction's launches are captured
+ * into a CUDA graph on first use on a non-default stream and replayed.
+ */
+typedef struct paliwa_gb_batch paliwa_gb_batch;
+
+int paliwa_gb_batch_create(int ndim, int ngrids, const int64_t *levels,
+                           const int64_t *minimum_level,
+                           const int64_t *maximum_level, int dtype,
+                           int wavelet, void *const *grid_ptrs,
+                           paliwa_gb_batch **out);
+int paliwa_gb_batch_hierarchize(paliwa_gb_batch *batch, void *stream);
+int paliwa_gb_batch_dehierarchize(paliwa_gb_batch *batch, void *stream);
+/* enable != 0 (default): capture and replay CUDA graphs. */
+int paliwa_gb_batch_use_graphs(paliwa_gb_batch *batch, int enable);
+int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
+                         int64_t *launches_forward,
+                         int64_t *launches_inverse);
+/* Runs one direction (forward != 0: hierarchize) launch by launch with CUDA
+ * events around each launch, waits for it, and reports each launch's
+ * duration and algorithmic bytes (one read and one write of every grid point
+ * it stores). Call with capacity 0 to get *nlaunches first. */
+int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
+                            int capacity, int *nlaunches, float *ms,
+                            int64_t *bytes);
+void paliwa_gb_batch_destroy(paliwa_gb_batch *batch);
+
+/* ------------------------------------------------------------------------
+ * Combination technique: sparse-grid combine, restrict and full-grid scatter
+ * in FP64. Restates test/test_paliwa_combination_technique.cpp:176-318
+ * (there only a test driver): every hierarchical subspace 0 <= s <= l of
+ * every grid is counted (paliwa/paliwa_utils.hpp:9-26); subspaces present in
+ * more than one grid are kept (keep_all != 0 keeps all), ordered
+ * lexicographically, each stored densely over the extents of
+ * paliwa::strided_hierarchical_domain_from_level(s, maximum_level)
+ * (paliwa/paliwa_domains.hpp:51-83), concatenated.
+ */
+typedef struct paliwa_gb_ct paliwa_gb_ct;
+
+int paliwa_gb_ct_create(int ndim, int ngrids, const int64_t *levels,
+                        const double *coefficients,
+                        const int64_t *maximum_level, int dtype,
+                        void *const *grid_ptrs, int keep_all,
+                        paliwa_gb_ct **out);
+int paliwa_gb_ct_info(const paliwa_gb_ct *ct, int64_t *npoints,
+                      int64_t *nsubspaces);
+/* levels: nsubspaces * ndim; offsets: nsubspaces (first point of each). */
+int paliwa_gb_ct_subspaces(const paliwa_gb_ct *ct, int64_t *levels,
+                           int64_t *offsets);
+/* sparse[p] = sum over grids g containing the subspace, in grid order, of
+ * coefficient_g * grid_g[p] (:256-290). sparse is device memory of npoints
+ * doubles; it is overwritten. */
+int paliwa_gb_ct_combine(paliwa_gb_ct *ct, double *sparse, void *stream);
+/* Writes each kept subspace's combined value into every grid containing it
+ * (rounded to the grid's storage type). */
+int paliwa_gb_ct_restrict(paliwa_gb_ct *ct, const double *sparse,
+                          void *stream);
+/* full = 0, then full[subspace points] += sparse (:293-318); full is the
+ * dense grid at maximum_level (2^sum(maximum_level) doubles). */
+int paliwa_gb_ct_scatter(paliwa_gb_ct *ct, const double *sparse, double *full,
+                         void *stream);
+void paliwa_gb_ct_destroy(paliwa_gb_ct *ct);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,26 @@ SIGNATURES = {
         _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _i, _vp]),
     "paliwa_gb_hierarchize": (_i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _vp]),
     "paliwa_gb_dehierarchize": (_i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _vp]),
+    "paliwa_gb_batch_create": (
+        _i, [_i, _i, _pi64, _pi64, _pi64, _i, _i, ctypes.POINTER(_vp),
+             ctypes.POINTER(_vp)]),
+    "paliwa_gb_batch_hierarchize": (_i, [_vp, _vp]),
+    "paliwa_gb_batch_dehierarchize": (_i, [_vp, _vp]),
+    "paliwa_gb_batch_use_graphs": (_i, [_vp, _i]),
+    "paliwa_gb_batch_info": (_i, [_vp, _pi64, _pi64, _pi64]),
+    "paliwa_gb_batch_profile": (
+        _i, [_vp, _i, _vp, _i, ctypes.POINTER(_i),
+             ctypes.POINTER(ctypes.c_float), _pi64]),
+    "paliwa_gb_batch_destroy": (None, [_vp]),
+    "paliwa_gb_ct_create": (
+        _i, [_i, _i, _pi64, _pd, _pi64, _i, ctypes.POINTER(_vp), _i,
+             ctypes.POINTER(_vp)]),
+    "paliwa_gb_ct_info": (_i, [_vp, _pi64, _pi64]),
+    "paliwa_gb_ct_subspaces": (_i, [_vp, _pi64, _pi64]),
+    "paliwa_gb_ct_combine": (_i, [_vp, _vp, _vp]),
+    "paliwa_gb_ct_restrict": (_i, [_vp, _vp, _vp]),
+    "paliwa_gb_ct_scatter": (_i, [_vp, _vp, _vp, _vp]),
+    "paliwa_gb_ct_destroy": (None, [_vp]),
 }
 
 

@@ -1,0 +1,525 @@
+// Batched transforms of many component grids and the combination-technique
+// combine / restrict / scatter (include/paliwa_gb300.h).
+//
+// The reference transforms the component grids of a combination scheme one
+// hierarchize() call each, spread over execution-space instances
+// (test/test_paliwa_combination_technique.cpp:164-174). Here one plan covers
+// every grid: for each axis, the per-grid stages of plan_axis() are merged
+// into one launch per stage index and chunk size, whose device-side job list
+// names every grid. The launch sequence of a direction is captured once into
+// a CUDA graph and replayed.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "combine.cuh"
+#include "paliwa_gb300.h"
+#include "plan.hpp"
+
+using namespace pgb;
+
+namespace {
+
+struct Launch {
+  int R = 0;
+  size_t job_first = 0;  // index into the device job array
+  int njobs = 0;
+  long long tiles = 0;
+  long long points = 0;  // grid points stored by this launch
+};
+
+struct Direction {
+  LiftParams params{};
+  bool exact = true;
+  std::vector<Launch> launches;
+  LiftJob *jobs_dev = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+};
+
+void free_direction(Direction &d) {
+  if (d.graph) cudaGraphExecDestroy(d.graph);
+  if (d.jobs_dev) cudaFree(d.jobs_dev);
+  d.graph = nullptr;
+  d.jobs_dev = nullptr;
+}
+
+void check_grid_levels(int ndim, int ngrids, int64_t const *levels,
+                       int64_t const *lmin, int64_t const *lmax) {
+  if (ndim < 1 || ndim > kMaxDims)
+    throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "ndim must be in [1, 12]");
+  if (ngrids < 1)
+    throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "no grids");
+  for (int g = 0; g < ngrids; ++g) {
+    int64_t total = 0;
+    for (int d = 0; d < ndim; ++d) {
+      int64_t const l = levels[g * ndim + d];
+      if (l < 0 || l > lmax[d] || lmax[d] > 30 ||
+          (lmin != nullptr && (lmin[d] < 0 || lmin[d] > l)))
+        throw StatusError(
+            PALIWA_GB_INVALID_ARGUMENT,
+            "requires 0 <= minimum_level <= level <= maximum_level <= 30");
+      total += l;
+    }
+    if (total > 40)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "grid too large");
+  }
+}
+
+} // namespace
+
+struct paliwa_gb_batch {
+  int ndim = 0;
+  int ngrids = 0;
+  int dtype = 0;
+  int wavelet = 0;
+  long long points = 0;
+  bool use_graphs = true;
+  Direction dir[2];  // 0 = forward, 1 = inverse
+};
+
+namespace {
+
+void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
+                    int64_t const *levels, int64_t const *lmin,
+                    void *const *grid_ptrs) {
+  auto const filters = wavelet_filters(b.wavelet, forward);
+  dr.params = launch_params(filters);
+  dr.exact = exact_scalers(filters);
+  std::vector<LiftJob> all_jobs;
+  for (int d = 0; d < b.ndim; ++d) {
+    // stages[g] = the ordered stages of grid g along axis d
+    std::vector<std::vector<Stage>> stages(b.ngrids);
+    size_t depth = 0;
+    for (int g = 0; g < b.ngrids; ++g) {
+      int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
+      plan_axis(axis_view(reinterpret_cast<unsigned long long>(grid_ptrs[g]),
+                          b.ndim, lv, d),
+                level_shifts(lv[d], lmin[d], forward), filters, stages[g]);
+      depth = std::max(depth, stages[g].size());
+    }
+    for (size_t k = 0; k < depth; ++k) {
+      // One launch per chunk size among the k-th stages of every grid.
+      std::map<int, std::vector<Stage const *>> by_r;
+      for (int g = 0; g < b.ngrids; ++g)
+        if (k < stages[g].size()) by_r[stages[g][k].R].push_back(&stages[g][k]);
+      for (auto const &[R, list] : by_r) {
+        Launch L;
+        L.R = R;
+        L.job_first = all_jobs.size();
+        L.njobs = static_cast<int>(list.size());
+        for (Stage const *st : list) {
+          LiftJob job = st->job;
+          job.tile_begin = L.tiles;
+          L.tiles += st->tiles;
+          L.points += st->job.columns << st->job.log2_n;
+          all_jobs.push_back(job);
+        }
+        if (L.R >= 2 && L.tiles > 0) dr.launches.push_back(L);
+      }
+    }
+  }
+  if (!all_jobs.empty()) {
+    size_t const bytes = all_jobs.size() * sizeof(LiftJob);
+    cuda_check(cudaMalloc(&dr.jobs_dev, bytes), "cudaMalloc(jobs)");
+    cuda_check(cudaMemcpy(dr.jobs_dev, all_jobs.data(), bytes,
+                          cudaMemcpyHostToDevice),
+               "cudaMemcpy(jobs)");
+  }
+}
+
+void run_direction(paliwa_gb_batch &b, Direction &dr, cudaStream_t s) {
+  auto launch_all = [&] {
+    for (auto const &L : dr.launches)
+      launch_lift(b.dtype, dr.exact, L.R, dr.params, dr.jobs_dev + L.job_first,
+                  L.njobs, L.tiles, s);
+  };
+  cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+  if (s != nullptr)
+    cuda_check(cudaStreamIsCapturing(s, &status), "cudaStreamIsCapturing");
+  // The legacy default stream cannot be captured; a stream that is already
+  // capturing records our launches into the caller's graph.
+  if (!b.use_graphs || s == nullptr || status != cudaStreamCaptureStatusNone) {
+    launch_all();
+    return;
+  }
+  if (dr.graph == nullptr) {
+    cudaGraph_t graph = nullptr;
+    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+               "cudaStreamBeginCapture");
+    try {
+      launch_all();
+    } catch (...) {
+      cudaStreamEndCapture(s, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    cuda_check(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
+    cudaError_t const e = cudaGraphInstantiate(&dr.graph, graph, 0);
+    cudaGraphDestroy(graph);
+    cuda_check(e, "cudaGraphInstantiate");
+  }
+  cuda_check(cudaGraphLaunch(dr.graph, s), "cudaGraphLaunch");
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// Combination technique.
+
+struct paliwa_gb_ct {
+  int ndim = 0;
+  int ngrids = 0;
+  int dtype = 0;
+  long long npoints = 0;
+  std::vector<std::vector<int>> subspace_levels;  // lexicographic order
+  std::vector<long long> offsets;
+  CtSubspace *subspaces_dev = nullptr;
+  int *lists_dev = nullptr;
+  CtGrid *grids_dev = nullptr;
+  CtParams params{};
+};
+
+namespace {
+
+// Key of a level vector (<= 12 dims, levels <= 30: 5 bits each).
+uint64_t level_key(int const *s, int ndim) {
+  uint64_t k = 0;
+  for (int d = 0; d < ndim; ++d) k = (k << 5) | static_cast<uint64_t>(s[d]);
+  return k;
+}
+
+void build_ct(paliwa_gb_ct &ct, int64_t const *levels,
+              double const *coefficients, int64_t const *lmax,
+              void *const *grid_ptrs, int keep_all) {
+  int const nd = ct.ndim;
+  // Count every hierarchical subspace 0 <= s <= l of every grid
+  // (paliwa_utils.hpp:9-26; test_paliwa_combination_technique.cpp:177-192).
+  std::unordered_map<uint64_t, int> count;
+  std::vector<int> s(nd);
+  for (int g = 0; g < ct.ngrids; ++g) {
+    int64_t const *lv = levels + static_cast<size_t>(g) * nd;
+    std::fill(s.begin(), s.end(), 0);
+    while (true) {
+      ++count[level_key(s.data(), nd)];
+      int d = nd - 1;
+      while (d >= 0 && s[d] == lv[d]) s[d--] = 0;
+      if (d < 0) break;
+      ++s[d];
+    }
+  }
+  // Keep subspaces present in more than one grid (:212-225), ordered like
+  // the reference's std::map (lexicographic on the level vector).
+  std::vector<std::vector<int>> kept;
+  for (auto const &[key, c] : count) {
+    if (c <= 1 && !keep_all) continue;
+    std::vector<int> v(nd);
+    uint64_t k = key;
+    for (int d = nd - 1; d >= 0; --d) {
+      v[d] = static_cast<int>(k & 31);
+      k >>= 5;
+    }
+    kept.push_back(v);
+  }
+  std::sort(kept.begin(), kept.end());
+  std::vector<CtSubspace> subs(kept.size());
+  std::vector<int> lists;
+  long long off = 0;
+  for (size_t i = 0; i < kept.size(); ++i) {
+    CtSubspace &ss = subs[i];
+    std::memset(&ss, 0, sizeof(ss));
+    ss.offset = off;
+    long long size = 1;
+    for (int d = 0; d < nd; ++d) {
+      ss.level[d] = static_cast<signed char>(kept[i][d]);
+      if (kept[i][d] > 0) size <<= (kept[i][d] - 1);
+    }
+    off += size;
+    ss.grid_begin = static_cast<int>(lists.size());
+    for (int g = 0; g < ct.ngrids; ++g) {
+      bool contains = true;  // :270-276
+      for (int d = 0; d < nd; ++d)
+        if (kept[i][d] > levels[static_cast<size_t>(g) * nd + d]) {
+          contains = false;
+          break;
+        }
+      if (contains) lists.push_back(g);
+    }
+    ss.grid_end = static_cast<int>(lists.size());
+  }
+  ct.npoints = off;
+  ct.subspace_levels = kept;
+  ct.offsets.resize(kept.size());
+  for (size_t i = 0; i < kept.size(); ++i) ct.offsets[i] = subs[i].offset;
+  std::vector<CtGrid> grids(ct.ngrids);
+  for (int g = 0; g < ct.ngrids; ++g) {
+    std::memset(&grids[g], 0, sizeof(CtGrid));
+    grids[g].base = reinterpret_cast<unsigned long long>(grid_ptrs[g]);
+    grids[g].coefficient = coefficients[g];
+    for (int d = 0; d < nd; ++d)
+      grids[g].level[d] =
+          static_cast<signed char>(levels[static_cast<size_t>(g) * nd + d]);
+  }
+  auto upload = [](auto **dst, auto const &v, char const *what) {
+    if (v.empty()) return;
+    size_t const bytes = v.size() * sizeof(v[0]);
+    cuda_check(cudaMalloc(reinterpret_cast<void **>(dst), bytes), what);
+    cuda_check(cudaMemcpy(*dst, v.data(), bytes, cudaMemcpyHostToDevice),
+               what);
+  };
+  upload(&ct.subspaces_dev, subs, "upload subspaces");
+  upload(&ct.lists_dev, lists, "upload grid lists");
+  upload(&ct.grids_dev, grids, "upload grids");
+  std::memset(&ct.params, 0, sizeof(ct.params));
+  ct.params.subspaces = ct.subspaces_dev;
+  ct.params.nsubspaces = static_cast<int>(subs.size());
+  ct.params.grid_lists = ct.lists_dev;
+  ct.params.grids = ct.grids_dev;
+  ct.params.ndim = nd;
+  ct.params.npoints = ct.npoints;
+  for (int d = 0; d < nd && d < kMaxDims; ++d)
+    ct.params.max_level[d] = static_cast<signed char>(lmax[d]);
+}
+
+template <int OP>
+void ct_launch(paliwa_gb_ct const &ct, double *sparse, double *full,
+               cudaStream_t s) {
+  if (ct.npoints == 0) return;
+  CtParams p = ct.params;
+  p.sparse = sparse;
+  p.full = full;
+  unsigned const blocks = static_cast<unsigned>((ct.npoints + 255) / 256);
+  switch (ct.dtype) {
+  case PALIWA_GB_F64: ct_kernel<double, OP><<<blocks, 256, 0, s>>>(p); break;
+  case PALIWA_GB_F32:
+  case PALIWA_GB_F32C: ct_kernel<float, OP><<<blocks, 256, 0, s>>>(p); break;
+  default: throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
+  }
+  cuda_check(cudaGetLastError(), "ct_kernel launch");
+}
+
+} // namespace
+
+extern "C" {
+
+int paliwa_gb_batch_create(int ndim, int ngrids, const int64_t *levels,
+                           const int64_t *minimum_level,
+                           const int64_t *maximum_level, int dtype,
+                           int wavelet, void *const *grid_ptrs,
+                           paliwa_gb_batch **out) {
+  return guarded([&] {
+    if (out == nullptr || levels == nullptr || minimum_level == nullptr ||
+        maximum_level == nullptr || grid_ptrs == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    check_grid_levels(ndim, ngrids, levels, minimum_level, maximum_level);
+    size_t const es = dtype_size(dtype);
+    wavelet_filters(wavelet, true);  // validates the id
+    auto b = std::make_unique<paliwa_gb_batch>();
+    b->ndim = ndim;
+    b->ngrids = ngrids;
+    b->dtype = dtype;
+    b->wavelet = wavelet;
+    for (int g = 0; g < ngrids; ++g) {
+      if (grid_ptrs[g] == nullptr ||
+          reinterpret_cast<uintptr_t>(grid_ptrs[g]) % es != 0)
+        throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                          "grid pointer is null or misaligned");
+      int64_t total = 0;
+      for (int d = 0; d < ndim; ++d) total += levels[g * ndim + d];
+      b->points += 1LL << total;
+    }
+    try {
+      plan_direction(*b, b->dir[0], true, levels, minimum_level, grid_ptrs);
+      plan_direction(*b, b->dir[1], false, levels, minimum_level, grid_ptrs);
+    } catch (...) {
+      free_direction(b->dir[0]);
+      free_direction(b->dir[1]);
+      throw;
+    }
+    *out = b.release();
+  });
+}
+
+int paliwa_gb_batch_hierarchize(paliwa_gb_batch *batch, void *stream) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    run_direction(*batch, batch->dir[0], static_cast<cudaStream_t>(stream));
+  });
+}
+
+int paliwa_gb_batch_dehierarchize(paliwa_gb_batch *batch, void *stream) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    run_direction(*batch, batch->dir[1], static_cast<cudaStream_t>(stream));
+  });
+}
+
+int paliwa_gb_batch_use_graphs(paliwa_gb_batch *batch, int enable) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    batch->use_graphs = enable != 0;
+  });
+}
+
+int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
+                         int64_t *launches_forward,
+                         int64_t *launches_inverse) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    if (points) *points = batch->points;
+    if (launches_forward)
+      *launches_forward = static_cast<int64_t>(batch->dir[0].launches.size());
+    if (launches_inverse)
+      *launches_inverse = static_cast<int64_t>(batch->dir[1].launches.size());
+  });
+}
+
+int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
+                            int capacity, int *nlaunches, float *ms,
+                            int64_t *bytes) {
+  return guarded([&] {
+    if (batch == nullptr || nlaunches == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    Direction &dr = batch->dir[forward ? 0 : 1];
+    cudaStream_t const s = static_cast<cudaStream_t>(stream);
+    int const n = static_cast<int>(dr.launches.size());
+    *nlaunches = n;
+    if (capacity < n || ms == nullptr || bytes == nullptr) return;
+    std::vector<cudaEvent_t> ev(n + 1);
+    for (auto &e : ev) cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    size_t const es = dtype_size(batch->dtype);
+    cuda_check(cudaEventRecord(ev[0], s), "cudaEventRecord");
+    for (int i = 0; i < n; ++i) {
+      Launch const &L = dr.launches[i];
+      launch_lift(batch->dtype, dr.exact, L.R, dr.params,
+                  dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
+      cuda_check(cudaEventRecord(ev[i + 1], s), "cudaEventRecord");
+      bytes[i] = static_cast<int64_t>(2 * es) * L.points;
+    }
+    cuda_check(cudaEventSynchronize(ev[n]), "cudaEventSynchronize");
+    for (int i = 0; i < n; ++i)
+      cuda_check(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]),
+                 "cudaEventElapsedTime");
+    for (auto &e : ev) cudaEventDestroy(e);
+  });
+}
+
+void paliwa_gb_batch_destroy(paliwa_gb_batch *batch) {
+  if (batch == nullptr) return;
+  free_direction(batch->dir[0]);
+  free_direction(batch->dir[1]);
+  delete batch;
+}
+
+int paliwa_gb_ct_create(int ndim, int ngrids, const int64_t *levels,
+                        const double *coefficients,
+                        const int64_t *maximum_level, int dtype,
+                        void *const *grid_ptrs, int keep_all,
+                        paliwa_gb_ct **out) {
+  return guarded([&] {
+    if (out == nullptr || levels == nullptr || coefficients == nullptr ||
+        maximum_level == nullptr || grid_ptrs == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    check_grid_levels(ndim, ngrids, levels, nullptr, maximum_level);
+    size_t const es = dtype_size(dtype);
+    for (int g = 0; g < ngrids; ++g)
+      if (grid_ptrs[g] == nullptr ||
+          reinterpret_cast<uintptr_t>(grid_ptrs[g]) % es != 0)
+        throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                          "grid pointer is null or misaligned");
+    auto ct = std::make_unique<paliwa_gb_ct>();
+    ct->ndim = ndim;
+    ct->ngrids = ngrids;
+    ct->dtype = dtype;
+    try {
+      build_ct(*ct, levels, coefficients, maximum_level, grid_ptrs, keep_all);
+    } catch (...) {
+      cudaFree(ct->subspaces_dev);
+      cudaFree(ct->lists_dev);
+      cudaFree(ct->grids_dev);
+      throw;
+    }
+    *out = ct.release();
+  });
+}
+
+int paliwa_gb_ct_info(const paliwa_gb_ct *ct, int64_t *npoints,
+                      int64_t *nsubspaces) {
+  return guarded([&] {
+    if (ct == nullptr) throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null ct");
+    if (npoints) *npoints = ct->npoints;
+    if (nsubspaces)
+      *nsubspaces = static_cast<int64_t>(ct->subspace_levels.size());
+  });
+}
+
+int paliwa_gb_ct_subspaces(const paliwa_gb_ct *ct, int64_t *levels,
+                           int64_t *offsets) {
+  return guarded([&] {
+    if (ct == nullptr) throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null ct");
+    for (size_t i = 0; i < ct->subspace_levels.size(); ++i) {
+      if (levels)
+        for (int d = 0; d < ct->ndim; ++d)
+          levels[i * ct->ndim + d] = ct->subspace_levels[i][d];
+      if (offsets) offsets[i] = ct->offsets[i];
+    }
+  });
+}
+
+int paliwa_gb_ct_combine(paliwa_gb_ct *ct, double *sparse, void *stream) {
+  return guarded([&] {
+    if (ct == nullptr || sparse == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    ct_launch<kCombine>(*ct, sparse, nullptr,
+                        static_cast<cudaStream_t>(stream));
+  });
+}
+
+int paliwa_gb_ct_restrict(paliwa_gb_ct *ct, const double *sparse,
+                          void *stream) {
+  return guarded([&] {
+    if (ct == nullptr || sparse == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    ct_launch<kRestrict>(*ct, const_cast<double *>(sparse), nullptr,
+                         static_cast<cudaStream_t>(stream));
+  });
+}
+
+int paliwa_gb_ct_scatter(paliwa_gb_ct *ct, const double *sparse, double *full,
+                         void *stream) {
+  return guarded([&] {
+    if (ct == nullptr || sparse == nullptr || full == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    // The full grid starts from zero (test_paliwa_combination_technique.cpp
+    // :295-298); every kept subspace point is then added once.
+    long long total = 0;
+    for (int d = 0; d < ct->ndim; ++d) total += ct->params.max_level[d];
+    if (total > 36)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "full grid too large");
+    cuda_check(cudaMemsetAsync(full, 0, sizeof(double) << total,
+                               static_cast<cudaStream_t>(stream)),
+               "cudaMemsetAsync");
+    ct_launch<kScatter>(*ct, const_cast<double *>(sparse), full,
+                        static_cast<cudaStream_t>(stream));
+  });
+}
+
+void paliwa_gb_ct_destroy(paliwa_gb_ct *ct) {
+  if (ct == nullptr) return;
+  cudaFree(ct->subspaces_dev);
+  cudaFree(ct->lists_dev);
+  cudaFree(ct->grids_dev);
+  delete ct;
+}
+
+} // extern "C"

@@ -44,60 +44,121 @@ bool exact_scalers(std::vector<Filter> const &filters) {
 
 int chunk_for(int log2_n) {
   if (log2_n <= 4) return 1 << log2_n;  // whole pencil in one thread
-  if (log2_n <= 12) return 16;
-  return 32;                              // 8192-point pencils
+  return 16;
+}
+
+void cuda_check(cudaError_t e, char const *what) {
+  if (e != cudaSuccess)
+    throw StatusError(PALIWA_GB_CUDA_ERROR,
+                      std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+size_t dtype_size(int dtype) {
+  switch (dtype) {
+  case PALIWA_GB_F64: return 8;
+  case PALIWA_GB_F32:
+  case PALIWA_GB_F32C: return 4;
+  }
+  throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
+}
+
+AxisView axis_view(unsigned long long base, int ndim, int64_t const *level,
+                   int dim) {
+  AxisView v;
+  int log2_outer = 0, log2_inner = 0;
+  for (int d = 0; d < dim; ++d) log2_outer += static_cast<int>(level[d]);
+  for (int d = dim + 1; d < ndim; ++d) log2_inner += static_cast<int>(level[d]);
+  v.base = base;
+  v.columns = 1LL << (log2_outer + log2_inner);
+  v.log2_inner = log2_inner;
+  v.log2_kstride = log2_inner;
+  v.log2_n = static_cast<int>(level[dim]);
+  v.log2_astride = v.log2_n + log2_inner;
+  return v;
+}
+
+std::vector<int> level_shifts(int64_t lev, int64_t lmin, bool forward) {
+  std::vector<int> sh;
+  // hierarchize_in: levels lev .. lmin+1 (paliwa_transform.hpp:364-367);
+  // dehierarchize_in: lmin+1 .. lev (:392-394). shift = lev - l.
+  for (int64_t l = lmin + 1; l <= lev; ++l)
+    sh.push_back(static_cast<int>(lev - l));
+  // sh now follows increasing levels (the inverse order).
+  if (forward) std::reverse(sh.begin(), sh.end());
+  return sh;
+}
+
+LiftParams launch_params(std::vector<Filter> const &filters) {
+  if (filters.size() > static_cast<size_t>(kMaxPasses))
+    throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "at most 8 filter passes");
+  LiftParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.npasses = static_cast<int>(filters.size());
+  p.fp64_log2_points = 2;
+  for (size_t i = 0; i < filters.size(); ++i) {
+    if (filters[i].offset != 0 && filters[i].offset != 1)
+      throw StatusError(PALIWA_GB_RUNTIME_ERROR, "Filter offset not supported");
+    p.offsets[i] = filters[i].offset;
+    p.coeffs[i] = {filters[i].c[0], filters[i].c[1], filters[i].c[2]};
+    if (filters[i].c[1] == 1.0) p.c1_one_mask |= 1u << i;
+  }
+  return p;
 }
 
 namespace {
 
 long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
-void fill_job(LiftJob &job, AxisView const &v, std::vector<int> const &sh,
-              size_t first, size_t count) {
-  job.offset = v.offset;
+LiftJob make_job(AxisView const &v, std::vector<int> const &sh, size_t first,
+                 size_t count) {
+  LiftJob job;
+  std::memset(&job, 0, sizeof(job));
+  job.base = v.base;
   job.columns = v.columns;
   job.tile_begin = 0;
   job.log2_inner = v.log2_inner;
   job.log2_kstride = v.log2_kstride;
   job.log2_astride = v.log2_astride;
   job.log2_n = v.log2_n;
-  job.seg_len = 0;
-  job.halo = 0;
   job.nlevels = static_cast<int>(count);
   for (size_t i = 0; i < count; ++i)
     job.shift[i] = static_cast<signed char>(sh[first + i]);
+  return job;
 }
 
-// Periodic whole-pencil launches; level lists longer than one job holds are
-// split into consecutive launches (order preserved).
+// Periodic whole-pencil stages; level lists longer than one job holds are
+// split into consecutive stages (order preserved).
 void plan_periodic(AxisView const &v, std::vector<int> const &shifts,
-                   LaunchPlan const &proto, std::vector<LaunchPlan> &out) {
+                   std::vector<Stage> &out) {
   int const R = chunk_for(v.log2_n);
   int const log2G = v.log2_n - (31 - __builtin_clz(R));
-  long long const C = kThreads >> log2G;
+  long long const C = static_cast<long long>(kRounds) * (kThreads >> log2G);
   for (size_t first = 0; first < shifts.size(); first += kMaxLevels) {
     size_t const count =
         std::min(shifts.size() - first, static_cast<size_t>(kMaxLevels));
-    LaunchPlan lp = proto;
-    lp.R = R;
-    lp.params.periodic = 1;
-    lp.params.log2_window = v.log2_n;
-    fill_job(lp.params.job, v, shifts, first, count);
-    lp.params.job.col_tiles = ceil_div(v.columns, C);
-    lp.tiles = lp.params.job.col_tiles;
-    out.push_back(lp);
+    Stage st;
+    st.R = R;
+    st.job = make_job(v, shifts, first, count);
+    st.job.periodic = 1;
+    st.job.log2_window = v.log2_n;
+    st.job.col_tiles = ceil_div(v.columns, C);
+    st.tiles = st.job.col_tiles;
+    out.push_back(st);
   }
 }
 
 // Fine levels of a long pencil on overlapping windows.
 void plan_windows(AxisView const &v, std::vector<int> const &shifts,
-                  std::vector<Filter> const &filters, LaunchPlan const &proto,
-                  std::vector<LaunchPlan> &out) {
+                  std::vector<Filter> const &filters,
+                  std::vector<Stage> &out) {
   long long const window = 1LL << kWindowLog2;
-  int const R = 32;
+  int const R = 16;
+  long long const C =
+      static_cast<long long>(kRounds) * (kThreads >> (kWindowLog2 - 4));
   size_t first = 0;
   while (first < shifts.size()) {
-    // Grow the run while the halo it needs fits the window.
+    // Grow the run while the halo it needs fits the window: each step of
+    // distance s widens the dependency cone by s on both sides.
     long long reach = 0;
     size_t count = 0;
     while (first + count < shifts.size() && count < kMaxLevels) {
@@ -113,16 +174,16 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
     if (seg_len <= 0)
       throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
                         "filter list too long for windowed long pencils");
-    LaunchPlan lp = proto;
-    lp.R = R;
-    lp.params.periodic = 0;
-    lp.params.log2_window = kWindowLog2;
-    fill_job(lp.params.job, v, shifts, first, count);
-    lp.params.job.seg_len = static_cast<int>(seg_len);
-    lp.params.job.halo = static_cast<int>(halo);
-    lp.params.job.col_tiles = v.columns;  // one column per CTA
-    lp.tiles = ceil_div(1LL << v.log2_n, seg_len) * v.columns;
-    out.push_back(lp);
+    Stage st;
+    st.R = R;
+    st.job = make_job(v, shifts, first, count);
+    st.job.periodic = 0;
+    st.job.log2_window = kWindowLog2;
+    st.job.seg_len = static_cast<int>(seg_len);
+    st.job.halo = static_cast<int>(halo);
+    st.job.col_tiles = ceil_div(v.columns, C);
+    st.tiles = ceil_div(1LL << v.log2_n, seg_len) * st.job.col_tiles;
+    out.push_back(st);
     first += count;
   }
 }
@@ -130,11 +191,10 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
 } // namespace
 
 void plan_axis(AxisView const &view, std::vector<int> const &shifts,
-               std::vector<Filter> const &filters, LaunchPlan const &proto,
-               std::vector<LaunchPlan> &out) {
+               std::vector<Filter> const &filters, std::vector<Stage> &out) {
   if (shifts.empty() || filters.empty() || view.log2_n == 0) return;
   if (view.log2_n <= kWindowLog2) {
-    plan_periodic(view, shifts, proto, out);
+    plan_periodic(view, shifts, out);
     return;
   }
   // Long pencil: levels closer than 2^m run on windows with a halo of at most
@@ -151,16 +211,83 @@ void plan_axis(AxisView const &view, std::vector<int> const &shifts,
     while (j < shifts.size() && (shifts[j] < m) == fine) ++j;
     std::vector<int> run(shifts.begin() + i, shifts.begin() + j);
     if (fine) {
-      plan_windows(view, run, filters, proto, out);
+      plan_windows(view, run, filters, out);
     } else {
       AxisView sub = view;
       sub.log2_n = view.log2_n - m;
       sub.log2_kstride = view.log2_kstride + m;
       for (int &s : run) s -= m;
-      plan_axis(sub, run, filters, proto, out);
+      plan_axis(sub, run, filters, out);
     }
     i = j;
   }
+}
+
+namespace {
+
+int device_sms() {
+  int dev = 0, sms = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+             "cudaDeviceGetAttribute");
+  return sms;
+}
+
+template <class A, int R>
+void launch_r(LiftParams const &p, cudaStream_t s) {
+  auto kernel = lift_kernel<A, R, kThreads>;
+  size_t const smem = lift_smem_bytes<A, R, kThreads>(kRounds);
+  static thread_local int per_sm = 0;
+  static thread_local int sms = 0;
+  if (per_sm == 0) {
+    cuda_check(cudaFuncSetAttribute(kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)),
+               "cudaFuncSetAttribute");
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &per_sm, kernel, kThreads, smem),
+               "occupancy query");
+    sms = device_sms();
+    if (per_sm < 1) per_sm = 1;
+  }
+  long long const resident = static_cast<long long>(per_sm) * sms;
+  long long const blocks = std::min(p.total_tiles, resident);
+  kernel<<<static_cast<unsigned>(blocks), kThreads, smem, s>>>(p);
+  cuda_check(cudaGetLastError(), "lift_kernel launch");
+}
+
+template <class A>
+void launch_a(int R, LiftParams const &p, cudaStream_t s) {
+  switch (R) {
+  case 2: return launch_r<A, 2>(p, s);
+  case 4: return launch_r<A, 4>(p, s);
+  case 8: return launch_r<A, 8>(p, s);
+  case 16: return launch_r<A, 16>(p, s);
+  }
+  throw StatusError(PALIWA_GB_RUNTIME_ERROR, "bad chunk size");
+}
+
+} // namespace
+
+void launch_lift(int dtype, bool exact, int R, LiftParams params,
+                 LiftJob const *jobs, int njobs, long long total_tiles,
+                 cudaStream_t s) {
+  if (total_tiles <= 0 || R < 2) return;
+  params.jobs = jobs;
+  params.njobs = njobs;
+  params.total_tiles = total_tiles;
+  params.rounds = kRounds;
+  switch (dtype) {
+  case PALIWA_GB_F64:
+    if (exact) return launch_a<Plain<double, true>>(R, params, s);
+    return launch_a<Plain<double, false>>(R, params, s);
+  case PALIWA_GB_F32:
+    if (exact) return launch_a<Plain<float, true>>(R, params, s);
+    return launch_a<Plain<float, false>>(R, params, s);
+  case PALIWA_GB_F32C:
+    return launch_a<Compensated>(R, params, s);
+  }
+  throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
 }
 
 } // namespace pgb
@@ -169,71 +296,13 @@ using namespace pgb;
 
 namespace {
 
-template <typename F> int guarded(F &&f) {
-  try {
-    f();
-    return PALIWA_GB_OK;
-  } catch (StatusError const &e) {
-    g_last_error = e.what();
-    return e.code;
-  } catch (std::exception const &e) {
-    g_last_error = e.what();
-    return PALIWA_GB_RUNTIME_ERROR;
-  }
-}
-
-void cuda_check(cudaError_t e, char const *what) {
-  if (e != cudaSuccess)
-    throw StatusError(PALIWA_GB_CUDA_ERROR,
-                      std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-template <class A>
-void launch_one(LaunchPlan const &lp, cudaStream_t s) {
-  dim3 const grid(static_cast<unsigned>(lp.tiles));
-  switch (lp.R) {
-  case 1: return;  // pencils of one point: nothing to do
-  case 2: lift_kernel<A, 2, kThreads><<<grid, kThreads, 0, s>>>(lp.params); break;
-  case 4: lift_kernel<A, 4, kThreads><<<grid, kThreads, 0, s>>>(lp.params); break;
-  case 8: lift_kernel<A, 8, kThreads><<<grid, kThreads, 0, s>>>(lp.params); break;
-  case 16: lift_kernel<A, 16, kThreads><<<grid, kThreads, 0, s>>>(lp.params); break;
-  case 32: lift_kernel<A, 32, kThreads><<<grid, kThreads, 0, s>>>(lp.params); break;
-  default: throw StatusError(PALIWA_GB_RUNTIME_ERROR, "bad chunk size");
-  }
-  cuda_check(cudaGetLastError(), "lift_kernel launch");
-}
-
-void launch(int dtype, bool exact, LaunchPlan const &lp, cudaStream_t s) {
-  if (lp.tiles <= 0) return;
-  if (lp.tiles > 0x7fffffffLL)
-    throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "grid too large");
-  switch (dtype) {
-  case PALIWA_GB_F64:
-    if (exact) return launch_one<Plain<double, true>>(lp, s);
-    return launch_one<Plain<double, false>>(lp, s);
-  case PALIWA_GB_F32:
-    if (exact) return launch_one<Plain<float, true>>(lp, s);
-    return launch_one<Plain<float, false>>(lp, s);
-  case PALIWA_GB_F32C:
-    return launch_one<Compensated>(lp, s);
-  }
-  throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
-}
-
-size_t dtype_size(int dtype) {
-  switch (dtype) {
-  case PALIWA_GB_F64: return 8;
-  case PALIWA_GB_F32:
-  case PALIWA_GB_F32C: return 4;
-  }
-  throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
-}
-
 void check_shape(void *grid, int dtype, int ndim, int64_t const *level,
                  int64_t const *maximum_level) {
   dtype_size(dtype);
   if (grid == nullptr)
     throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "grid is null");
+  if (reinterpret_cast<uintptr_t>(grid) % dtype_size(dtype) != 0)
+    throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "grid is misaligned");
   if (ndim < 1 || ndim > 32)
     throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "ndim must be in [1, 32]");
   long long total = 0;
@@ -249,60 +318,20 @@ void check_shape(void *grid, int dtype, int ndim, int64_t const *level,
     throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "grid too large");
 }
 
-AxisView axis_view(int ndim, int64_t const *level, int dim) {
-  AxisView v;
-  int log2_outer = 0, log2_inner = 0;
-  for (int d = 0; d < dim; ++d) log2_outer += static_cast<int>(level[d]);
-  for (int d = dim + 1; d < ndim; ++d) log2_inner += static_cast<int>(level[d]);
-  v.offset = 0;
-  v.columns = 1LL << (log2_outer + log2_inner);
-  v.log2_inner = log2_inner;
-  v.log2_kstride = log2_inner;
-  v.log2_n = static_cast<int>(level[dim]);
-  v.log2_astride = v.log2_n + log2_inner;
-  return v;
-}
-
-LaunchPlan prototype(void *grid, std::vector<Filter> const &filters) {
-  if (filters.size() > static_cast<size_t>(kMaxPasses))
-    throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "at most 8 filter passes");
-  LaunchPlan lp;
-  std::memset(&lp.params, 0, sizeof(lp.params));
-  lp.params.data = grid;
-  lp.params.jobs = nullptr;
-  lp.params.njobs = 1;
-  lp.params.vec_ok = (reinterpret_cast<uintptr_t>(grid) % 16) == 0;
-  lp.params.npasses = static_cast<int>(filters.size());
-  lp.params.fp64_log2_points = 2;
-  for (size_t p = 0; p < filters.size(); ++p) {
-    if (filters[p].offset != 0 && filters[p].offset != 1)
-      throw StatusError(PALIWA_GB_RUNTIME_ERROR, "Filter offset not supported");
-    lp.params.offsets[p] = filters[p].offset;
-    lp.params.coeffs[p] = {filters[p].c[0], filters[p].c[1], filters[p].c[2]};
-    if (filters[p].c[1] == 1.0) lp.params.c1_one_mask |= 1u << p;
-  }
-  return lp;
-}
-
 void transform_axis(void *grid, int dtype, int ndim, int64_t const *level,
                     int dim, std::vector<int> const &shifts,
                     std::vector<Filter> const &filters, cudaStream_t s) {
-  LaunchPlan const proto = prototype(grid, filters);
-  std::vector<LaunchPlan> plans;
-  plan_axis(axis_view(ndim, level, dim), shifts, filters, proto, plans);
+  LiftParams const params = launch_params(filters);
+  std::vector<Stage> stages;
+  plan_axis(axis_view(reinterpret_cast<unsigned long long>(grid), ndim, level,
+                      dim),
+            shifts, filters, stages);
   bool const exact = exact_scalers(filters);
-  for (auto const &lp : plans) launch(dtype, exact, lp, s);
-}
-
-std::vector<int> level_shifts(int64_t lev, int64_t lmin, bool forward) {
-  std::vector<int> sh;
-  // hierarchize_in: levels lev .. lmin+1 (paliwa_transform.hpp:364-367);
-  // dehierarchize_in: lmin+1 .. lev (:392-394). shift = lev - l.
-  for (int64_t l = lmin + 1; l <= lev; ++l)
-    sh.push_back(static_cast<int>(lev - l));
-  // sh now follows increasing levels (the inverse order).
-  if (forward) std::reverse(sh.begin(), sh.end());
-  return sh;
+  for (auto const &st : stages) {
+    LiftParams p = params;
+    p.job = st.job;
+    launch_lift(dtype, exact, st.R, p, nullptr, 1, st.tiles, s);
+  }
 }
 
 void check_levels(int ndim, int64_t const *level, int64_t const *lmin,

@@ -35,17 +35,19 @@ constexpr int kMaxPasses = 8;
 constexpr int kMaxLevels = 48;
 
 // One unit of work for a launch: one grid (or one sub-lattice of a grid)
-// along one axis.
+// along one axis. Jobs of a launch are sorted by tile_begin.
 struct LiftJob {
-  long long offset;      // element offset of the grid in the data buffer
-  long long columns;     // outer * inner
-  long long tile_begin;  // index of the first CTA of this job in the launch
-  long long col_tiles;   // CTAs per window row (ceil(columns / C))
-  int log2_inner;        // inner extent: splits a column index into (a, b)
-  int log2_kstride;      // element stride between consecutive pencil points
-  int log2_astride;      // element stride between consecutive outer indices
-  int log2_n;            // pencil length of the whole (sub-lattice) axis
-  // Window mode (periodic == 0): the window covers points
+  unsigned long long base;  // byte address of the grid's first element
+  long long columns;        // outer * inner
+  long long tile_begin;     // index of the first tile of this job
+  long long col_tiles;      // tiles per window row (ceil(columns / C))
+  int log2_inner;           // inner extent: splits a column index into (a, b)
+  int log2_kstride;         // element stride between consecutive pencil points
+  int log2_astride;         // element stride between consecutive outer indices
+  int log2_n;               // pencil length of the whole (sub-lattice) axis
+  int log2_window;          // points per pencil held by one CTA
+  int periodic;             // 1: whole periodic pencils; 0: windows
+  // Window mode: the window covers points
   // [seg * seg_len - halo, seg * seg_len + seg_len + halo) of the pencil.
   int seg_len;
   int halo;
@@ -54,14 +56,12 @@ struct LiftJob {
 };
 
 struct LiftParams {
-  void *data;
   LiftJob const *jobs;  // device array, or nullptr to use `job`
   int njobs;
-  int log2_window;      // log2 of the points per pencil held by one CTA
-  int periodic;         // 1: whole periodic pencils; 0: windows
-  int vec_ok;           // 16-byte aligned contiguous chunks may be vectorized
+  long long total_tiles;
   int npasses;
   int fp64_log2_points; // steps updating <= 2^this points per pencil in FP64
+  int rounds;           // column rounds per tile (tile = rounds * NT * R)
   unsigned c1_one_mask;
   int offsets[kMaxPasses];
   Coeffs coeffs[kMaxPasses];
@@ -147,48 +147,169 @@ __device__ __forceinline__ V coarse_update(Coeffs const &cf, bool c1one,
   return A::template update<false, false>(cf, lo, me, up);
 }
 
-template <typename S, int R>
-__device__ __forceinline__ void load_chunk(S const *p, long long kstride,
-                                           bool vec, S (&out)[R]) {
-  constexpr int PER = 16 / sizeof(S);
-  if constexpr (R % PER == 0) {
-    if (vec) {
-#pragma unroll
-      for (int q = 0; q < R / PER; ++q) {
-        uint4 u = *reinterpret_cast<uint4 const *>(p + q * PER);
-        S tmp[PER];
-        memcpy(tmp, &u, 16);
-#pragma unroll
-        for (int e = 0; e < PER; ++e) out[q * PER + e] = tmp[e];
-      }
-      return;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < R; ++j) out[j] = p[j * kstride];
+// Warp shuffles of one value (double, float or a double-float pair).
+__device__ __forceinline__ double shfl(double x, int src) {
+  return __shfl_sync(0xffffffffu, x, src);
+}
+__device__ __forceinline__ float shfl(float x, int src) {
+  return __shfl_sync(0xffffffffu, x, src);
+}
+__device__ __forceinline__ DF shfl(DF x, int src) {
+  return {__shfl_sync(0xffffffffu, x.h, src),
+          __shfl_sync(0xffffffffu, x.l, src)};
 }
 
-template <typename S, int R>
-__device__ __forceinline__ void store_chunk(S *p, long long kstride, bool vec,
-                                            S const (&in)[R]) {
-  constexpr int PER = 16 / sizeof(S);
-  if constexpr (R % PER == 0) {
-    if (vec) {
+// Shared-memory staging layout of one tile: column w, chunk c, slot j at
+//   w * pitch + c * (R + 1) + j,   pitch = G * (R + 1) rounded up to odd.
+// The per-chunk pad makes the chunk reads of a warp (lanes = consecutive
+// chunks) conflict free; the odd column pitch makes the coalesced copy
+// (lanes = consecutive columns of one row) conflict free.
+template <int R>
+__device__ __forceinline__ int stage_pitch(int G) {
+  return (G * (R + 1)) | 1;
+}
+
+// Copies one tile between global memory and the staging layout.
+//
+// The tile is `cols` consecutive columns (global column index gc0 + w) by
+// 2^log2W pencil points. A column index splits into (a, b) with b < inner; the
+// point k of column (a, b) lives at element
+//   a * astride + b + pos(k) * kstride,  pos(k) = (wstart + k) mod n.
+// Three paths, chosen per tile (uniform over the CTA):
+//  * rows: memory rows of RL = min(inner, cols) >= VEC contiguous elements,
+//    copied as 16-byte vectors (strided axes);
+//  * pencils: inner == 1 and kstride == 1, each column contiguous along k,
+//    copied as 16-byte vectors (the last axis);
+//  * scalar: anything else (narrow inner extents, sub-lattices).
+// Stores (Store == true) keep only in-range columns and, for windows, the
+// points k in [halo, halo + seg_len) that fall inside the pencil.
+template <typename S, int R, int NT> struct TileCopy {
+  static constexpr int VEC = 16 / sizeof(S);
+  static constexpr int LOG2R = Log2<R>::value;
+  LiftJob const &job;
+  int periodic, log2W, cols, pitch;
+  long long gc0, wstart, n;
+  unsigned char *gbase;
+
+  __device__ TileCopy(LiftJob const &j, int per, int lw, int c, long long g0,
+                      long long ws, long long nn, int pt, unsigned char *gb)
+      : job(j), periodic(per), log2W(lw), cols(c), pitch(pt), gc0(g0),
+        wstart(ws), n(nn), gbase(gb) {}
+
+  __device__ __forceinline__ int sidx(int w, int k) const {
+    return w * pitch + (k >> LOG2R) * (R + 1) + (k & (R - 1));
+  }
+  __device__ __forceinline__ long long pos(int k) const {
+    long long p = wstart + k;
+    if (!periodic) {
+      p %= n;
+      if (p < 0) p += n;
+    }
+    return p;
+  }
+  __device__ __forceinline__ bool keep(long long seg, int k, int halo,
+                                       int seg_len) const {
+    if (periodic) return true;
+    return k >= halo && k < halo + seg_len &&
+           seg * seg_len + (k - halo) < n;
+  }
+
+  template <bool Store>
+  __device__ __forceinline__ void run(S *stage, int t, long long seg,
+                                      int halo, int seg_len) const {
+    int const log2B = job.log2_inner;
+    int const log2cols = 31 - __clz(cols);
+    S *const g = reinterpret_cast<S *>(gbase);
+    long long const columns = job.columns;
+    bool const aligned = (job.base & 15ull) == 0;
+    int const log2RL = log2B < log2cols ? log2B : log2cols;
+    if (aligned && VEC > 1 && (1 << log2RL) >= VEC) {
+      // rows of RL contiguous elements; row rho = (a_off, k)
+      int const log2vpr = log2RL - Log2<VEC>::value;
+      int const nvec = (cols << log2W) / VEC;
+      long long const a0 = gc0 >> log2B;
+      long long const b0 = gc0 & ((1LL << log2B) - 1);
+#pragma unroll 4
+      for (int v = t; v < nvec; v += NT) {
+        int const rho = v >> log2vpr;
+        int const q = v & ((1 << log2vpr) - 1);
+        int const k = rho & ((1 << log2W) - 1);
+        int const a_off = rho >> log2W;
+        int const w0 = (a_off << log2RL) + q * VEC;
+        if (gc0 + w0 >= columns) continue;  // whole vector out of range
+        if (Store && !keep(seg, k, halo, seg_len)) continue;
+        long long const off = ((a0 + a_off) << job.log2_astride) + b0 +
+                              (pos(k) << job.log2_kstride) + q * VEC;
+        int const sb = sidx(w0, k);
+        if constexpr (Store) {
+          S tmp[VEC];
 #pragma unroll
-      for (int q = 0; q < R / PER; ++q) {
-        S tmp[PER];
+          for (int i = 0; i < VEC; ++i) tmp[i] = stage[sb + i * pitch];
+          uint4 u;
+          memcpy(&u, tmp, 16);
+          *reinterpret_cast<uint4 *>(g + off) = u;
+        } else {
+          uint4 const u = *reinterpret_cast<uint4 const *>(g + off);
+          S tmp[VEC];
+          memcpy(tmp, &u, 16);
 #pragma unroll
-        for (int e = 0; e < PER; ++e) tmp[e] = in[q * PER + e];
-        uint4 u;
-        memcpy(&u, tmp, 16);
-        *reinterpret_cast<uint4 *>(p + q * PER) = u;
+          for (int i = 0; i < VEC; ++i) stage[sb + i * pitch] = tmp[i];
+        }
       }
       return;
     }
-  }
+    if (aligned && VEC > 1 && log2B == 0 && job.log2_kstride == 0 &&
+        R >= VEC) {
+      // each column contiguous along k
+      int const log2vpc = log2W - Log2<VEC>::value;
+      int const nvec = (cols << log2W) / VEC;
+#pragma unroll 4
+      for (int v = t; v < nvec; v += NT) {
+        int const w = v >> log2vpc;
+        int const k = (v & ((1 << log2vpc) - 1)) * VEC;
+        if (gc0 + w >= columns) continue;
+        if (Store && !keep(seg, k, halo, seg_len)) continue;
+        long long const off = ((gc0 + w) << job.log2_astride) + pos(k);
+        int const sb = sidx(w, k);
+        if constexpr (Store) {
+          S tmp[VEC];
 #pragma unroll
-  for (int j = 0; j < R; ++j) p[j * kstride] = in[j];
-}
+          for (int i = 0; i < VEC; ++i) tmp[i] = stage[sb + i];
+          uint4 u;
+          memcpy(&u, tmp, 16);
+          *reinterpret_cast<uint4 *>(g + off) = u;
+        } else {
+          uint4 const u = *reinterpret_cast<uint4 const *>(g + off);
+          S tmp[VEC];
+          memcpy(tmp, &u, 16);
+#pragma unroll
+          for (int i = 0; i < VEC; ++i) stage[sb + i] = tmp[i];
+        }
+      }
+      return;
+    }
+    // scalar: elements ordered (a, k, b) with b fastest
+    int const log2Bb = log2B < log2cols ? log2B : log2cols;
+    int const total = cols << log2W;
+#pragma unroll 4
+    for (int e = t; e < total; e += NT) {
+      int const bo = e & ((1 << log2Bb) - 1);
+      int const k = (e >> log2Bb) & ((1 << log2W) - 1);
+      int const ao = e >> (log2Bb + log2W);
+      int const w = (ao << log2Bb) | bo;
+      long long const gc = gc0 + w;
+      if (gc >= columns) continue;
+      if (Store && !keep(seg, k, halo, seg_len)) continue;
+      long long const off = ((gc >> log2B) << job.log2_astride) +
+                            (gc & ((1LL << log2B) - 1)) +
+                            (pos(k) << job.log2_kstride);
+      if constexpr (Store)
+        g[off] = stage[sidx(w, k)];
+      else
+        stage[sidx(w, k)] = g[off];
+    }
+  }
+};
 
 template <class A, int R, int NT>
 __global__ void __launch_bounds__(NT)
@@ -197,128 +318,140 @@ __global__ void __launch_bounds__(NT)
   using S = typename A::Store;
   constexpr int LOG2R = Log2<R>::value;
   constexpr int LOG2NT = Log2<NT>::value;
-  __shared__ V heads[NT];
-  __shared__ V xch[2][NT];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *heads = reinterpret_cast<V *>(smem_raw);
+  V *xch = heads + NT;  // two buffers of NT
+  S *stage = reinterpret_cast<S *>(xch + 2 * NT);
 
-  long long const tile = blockIdx.x;
-  LiftJob const *job = &p.job;
-  if (p.jobs != nullptr) {
-    int lo = 0, hi = p.njobs - 1;
-    while (lo < hi) {
-      int const mid = (lo + hi + 1) >> 1;
-      if (p.jobs[mid].tile_begin <= tile)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    job = p.jobs + lo;
-  }
-  int const log2G = p.log2_window - LOG2R;
-  int const G = 1 << log2G;
-  int const log2C = LOG2NT - log2G;
   int const t = threadIdx.x;
-  int const col = t & ((1 << log2C) - 1);
-  int const c = t >> log2C;
-
-  long long const local = tile - job->tile_begin;
-  long long const seg = local / job->col_tiles;
-  long long const gc = (local - seg * job->col_tiles) * (1LL << log2C) + col;
-  bool const active = gc < job->columns;
-  int const log2B = job->log2_inner;
-  long long const a = gc >> log2B;
-  long long const b = gc & ((1LL << log2B) - 1);
-  long long const n = 1LL << job->log2_n;
-  long long const kstride = 1LL << job->log2_kstride;
-
-  // Position of this thread's chunk along the pencil.
-  long long pos = (long long)c * R;
-  bool store_me = active;
-  if (!p.periodic) {
-    long long const start = seg * job->seg_len - job->halo;
-    bool const in_segment =
-        pos >= job->halo && pos < job->halo + job->seg_len &&
-        seg * job->seg_len + (pos - job->halo) < n;
-    store_me = active && in_segment;
-    pos = (start + pos) % n;
-    if (pos < 0) pos += n;
-  }
-  S *g = static_cast<S *>(p.data) + job->offset + (a << job->log2_astride) +
-         b + pos * kstride;
-  bool const vec = p.vec_ok && job->log2_kstride == 0;
-
-  V v[R];
-  {
-    S raw[R];
-    if (active) {
-      load_chunk<S, R>(g, kstride, vec, raw);
-    } else {
-#pragma unroll
-      for (int j = 0; j < R; ++j) raw[j] = S(0);
+  int const lane = t & 31;
+  int ji = 0;
+  LiftJob const *job = p.jobs != nullptr ? p.jobs : &p.job;
+  // Persistent CTAs: tiles are visited in increasing order, so the job
+  // cursor only moves forward.
+  for (long long tile = blockIdx.x; tile < p.total_tiles; tile += gridDim.x) {
+    if (p.jobs != nullptr) {
+      while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
+      job = p.jobs + ji;
     }
-#pragma unroll
-    for (int j = 0; j < R; ++j) v[j] = A::load(raw[j]);
-  }
+    int const log2W = job->log2_window;       // points per column held
+    int const log2G = log2W - LOG2R;          // chunks per column
+    int const G = 1 << log2G;
+    int const log2CR = LOG2NT - log2G;        // columns per round
+    int const rounds = p.rounds;
+    int const cols = rounds << log2CR;        // columns per tile
+    int const pitch = stage_pitch<R>(G);
+    int const periodic = job->periodic;
+    long long const n = 1LL << job->log2_n;
 
-  bool heads_valid = false;
-  int buf = 0;
-  int const nlev = job->nlevels;
-  for (int li = 0; li < nlev; ++li) {
-    int const sh = job->shift[li];
-    // Points updated per pencil by one pass of this level: n / (2 s).
-    bool const f64 = (job->log2_n - sh - 1) <= p.fp64_log2_points;
-    for (int ps = 0; ps < p.npasses; ++ps) {
-      int const o = p.offsets[ps];
-      Coeffs const cf = p.coeffs[ps];
-      bool const c1one = (p.c1_one_mask >> ps) & 1u;
-      if (sh < LOG2R) {
-        V nb;
-        if (G > 1) {
-          xch[buf][t] = (o == 1) ? v[0] : tail_value<R>(v, sh);
-          __syncthreads();
-          int nc = (o == 1) ? c + 1 : c - 1;
-          if (p.periodic)
-            nc &= G - 1;
-          else
-            nc = nc < 0 ? 0 : (nc >= G ? G - 1 : nc);
-          nb = xch[buf][(nc << log2C) | col];
-          buf ^= 1;
-        } else {
-          nb = (o == 1) ? v[0] : tail_value<R>(v, sh);
-        }
-        fine_dispatch<A, R>(v, sh, o, nb, cf, c1one, f64);
-        if (o == 0) heads_valid = false;
-      } else {
-        if (!heads_valid) {
-          heads[t] = v[0];
-          __syncthreads();
-          heads_valid = true;
-        }
-        int const d = 1 << (sh - LOG2R);
-        if ((c & (2 * d - 1)) == o * d) {
-          int cl = c - d, cu = c + d;
-          if (p.periodic) {
-            cl &= G - 1;
-            cu &= G - 1;
+    long long const local = tile - job->tile_begin;
+    long long const seg = local / job->col_tiles;
+    long long const gc0 = (local - seg * job->col_tiles) * cols;
+    long long const wstart =
+        periodic ? 0 : seg * job->seg_len - job->halo;  // window origin
+
+    unsigned char *const gbase = reinterpret_cast<unsigned char *>(job->base);
+
+    __syncthreads();  // the previous tile is out of shared memory
+    // ---- load: global -> stage
+    TileCopy<S, R, NT> cp(*job, periodic, log2W, cols, gc0, wstart, n, pitch,
+                          gbase);
+    cp.template run<false>(stage, t, seg, 0, 0);
+    __syncthreads();
+
+    // ---- compute: one round = NT / G columns, thread = (column, chunk)
+    for (int r = 0; r < rounds; ++r) {
+      int const c = t & (G - 1);
+      int const wl = (r << log2CR) + (t >> log2G);
+      S *chunk = stage + wl * pitch + c * (R + 1);
+      V v[R];
+#pragma unroll
+      for (int j = 0; j < R; ++j) v[j] = A::load(chunk[j]);
+
+      // Lanes of one column inside a warp (G <= 32): shuffles only.
+      int const gbase_lane = lane & ~(G - 1);
+      bool heads_valid = false;
+      int buf = 0;
+      int const nlev = job->nlevels;
+      for (int li = 0; li < nlev; ++li) {
+        int const sh = job->shift[li];
+        bool const f64 = (job->log2_n - sh - 1) <= p.fp64_log2_points;
+        for (int ps = 0; ps < p.npasses; ++ps) {
+          int const o = p.offsets[ps];
+          Coeffs const cf = p.coeffs[ps];
+          bool const c1one = (p.c1_one_mask >> ps) & 1u;
+          if (sh < LOG2R) {
+            V nb;
+            V const pub = (o == 1) ? v[0] : tail_value<R>(v, sh);
+            if (G == 1) {
+              nb = pub;
+            } else if (G <= 32) {
+              int const nc = (o == 1) ? c + 1 : c - 1;
+              nb = shfl(pub, gbase_lane | (nc & (G - 1)));
+            } else {
+              xch[buf * NT + t] = pub;
+              __syncthreads();
+              int nc = (o == 1) ? c + 1 : c - 1;
+              if (periodic)
+                nc &= G - 1;
+              else
+                nc = nc < 0 ? 0 : (nc >= G ? G - 1 : nc);
+              nb = xch[buf * NT + ((t >> log2G) << log2G) + nc];
+              buf ^= 1;
+            }
+            fine_dispatch<A, R>(v, sh, o, nb, cf, c1one, f64);
+            if (o == 0) heads_valid = false;
           } else {
-            cl = cl < 0 ? c : cl;
-            cu = cu >= G ? c : cu;
+            int const d = 1 << (sh - LOG2R);
+            bool const mine = (c & (2 * d - 1)) == o * d;
+            if (G <= 32) {
+              V const lo = shfl(v[0], gbase_lane | ((c - d) & (G - 1)));
+              V const up = shfl(v[0], gbase_lane | ((c + d) & (G - 1)));
+              if (mine) v[0] = coarse_update<A>(cf, c1one, f64, lo, v[0], up);
+            } else {
+              if (!heads_valid) {
+                heads[t] = v[0];
+                __syncthreads();
+                heads_valid = true;
+              }
+              if (mine) {
+                int cl = c - d, cu = c + d;
+                if (periodic) {
+                  cl &= G - 1;
+                  cu &= G - 1;
+                } else {
+                  cl = cl < 0 ? c : cl;
+                  cu = cu >= G ? c : cu;
+                }
+                int const colbase = (t >> log2G) << log2G;
+                V const lo = heads[colbase + cl];
+                V const up = heads[colbase + cu];
+                v[0] = coarse_update<A>(cf, c1one, f64, lo, v[0], up);
+                heads[t] = v[0];
+              }
+              __syncthreads();
+            }
           }
-          V const lo = heads[(cl << log2C) | col];
-          V const up = heads[(cu << log2C) | col];
-          v[0] = coarse_update<A>(cf, c1one, f64, lo, v[0], up);
-          heads[t] = v[0];
         }
-        __syncthreads();
       }
-    }
-  }
-
-  if (store_me) {
-    S raw[R];
 #pragma unroll
-    for (int j = 0; j < R; ++j) raw[j] = A::store(v[j]);
-    store_chunk<S, R>(g, kstride, vec, raw);
+      for (int j = 0; j < R; ++j) chunk[j] = A::store(v[j]);
+      if (G > 32) __syncthreads();  // heads / xch reused by the next round
+    }
+    __syncthreads();
+
+    // ---- store: stage -> global (only this tile's segment of a window)
+    cp.template run<true>(stage, t, seg, job->halo, job->seg_len);
   }
+}
+
+// Dynamic shared memory of one CTA (an upper bound over every column shape:
+// cols * pitch <= rounds * NT * (R + 1) + cols and cols <= rounds * NT).
+template <class A, int R, int NT>
+constexpr size_t lift_smem_bytes(int rounds) {
+  using V = typename A::V;
+  using S = typename A::Store;
+  return 3 * NT * sizeof(V) + size_t(rounds) * NT * (R + 2) * sizeof(S);
 }
 
 } // namespace pgb

@@ -1,7 +1,7 @@
 // Host-side planning of the per-axis lifting launches.
 //
 // Turns "apply these levels (in this order) with these filters along axis
-// `dim` of a grid" into kernel launches (lift.cuh). This is where paliwa's
+// `dim` of a grid" into kernel jobs (lift.cuh). This is where paliwa's
 // level-strided index maps (paliwa/paliwa_domains.hpp:33-139:
 // strided_domain_from_level, even/odd half domains) become arithmetic on a
 // dense [outer][n][inner] view: level l of an axis at level `lev` has compact
@@ -31,36 +31,68 @@ struct Filter {
 
 // Wavelet tables, paliwa/paliwa_wavelets.hpp:15-28.
 std::vector<Filter> wavelet_filters(int wavelet, bool forward);
+bool exact_scalers(std::vector<Filter> const &filters);
 
 // A dense view of the pencils along one axis.
 struct AxisView {
-  long long offset = 0;  // element offset of the grid in the buffer
-  long long columns = 1; // outer * inner
+  unsigned long long base = 0;  // byte address of the grid
+  long long columns = 1;        // outer * inner
   int log2_inner = 0;
   int log2_kstride = 0;  // element stride between consecutive pencil points
   int log2_astride = 0;  // element stride between consecutive outer indices
   int log2_n = 0;        // pencil length
 };
 
-// A planned launch: kernel parameters with one inline job (single grid) or,
-// for batches, a job index range; the tile count; the register chunk R.
-struct LaunchPlan {
-  LiftParams params{};
+AxisView axis_view(unsigned long long base, int ndim, int64_t const *level,
+                   int dim);
+
+// One stage of an axis transform: a job for a kernel with chunk size R. The
+// stages of one axis must run in order; stages of different grids are
+// independent.
+struct Stage {
   int R = 0;
   long long tiles = 0;
-  // Jobs of a batched launch (params.jobs is set when uploaded).
-  std::vector<LiftJob> jobs;
+  LiftJob job{};
 };
 
-constexpr int kWindowLog2 = 13;     // points per pencil per CTA (8192)
+constexpr int kWindowLog2 = 12;   // points per column per CTA round (4096)
 constexpr int kThreads = 256;
-constexpr int kHaloBudget = 512;    // halo per side of a window, in points
+constexpr int kRounds = 2;        // column rounds per tile
+constexpr int kHaloBudget = 256;  // halo per side of a window, in points
 
-int chunk_for(int log2_n);          // R for a periodic pencil of 2^log2_n
+int chunk_for(int log2_n);        // R for a periodic pencil of 2^log2_n
 void plan_axis(AxisView const &view, std::vector<int> const &shifts,
-               std::vector<Filter> const &filters, LaunchPlan const &proto,
-               std::vector<LaunchPlan> &out);
+               std::vector<Filter> const &filters, std::vector<Stage> &out);
 
-bool exact_scalers(std::vector<Filter> const &filters);
+// Kernel-level parameters shared by every job of a launch.
+LiftParams launch_params(std::vector<Filter> const &filters);
+
+// Launch the lifting kernel for `dtype` over `njobs` jobs (device array
+// `jobs`, or the inline job of `params` when jobs == nullptr).
+void launch_lift(int dtype, bool exact, int R, LiftParams params,
+                 LiftJob const *jobs, int njobs, long long total_tiles,
+                 cudaStream_t stream);
+
+void cuda_check(cudaError_t e, char const *what);
+size_t dtype_size(int dtype);
+
+// Shifts (log2 distances) of hierarchize_in (forward: levels level..lmin+1)
+// or dehierarchize_in (lmin+1..level).
+std::vector<int> level_shifts(int64_t lev, int64_t lmin, bool forward);
+
+extern thread_local std::string g_last_error;
+
+template <typename F> int guarded(F &&f) {
+  try {
+    f();
+    return 0;
+  } catch (StatusError const &e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (std::exception const &e) {
+    g_last_error = e.what();
+    return 2;
+  }
+}
 
 } // namespace pgb

@@ -1,0 +1,244 @@
+"""Batched transforms and the sparse-grid combination technique.
+
+The reference ships the combination technique only as a test driver
+(test/test_paliwa_combination_technique.cpp:77-340): hierarchize every
+component grid, combine the hierarchical surpluses with the scheme's
+coefficients into the sparse-grid subspaces (FP64), scatter them onto a full
+grid and dehierarchize it. This module exposes those steps over the CUDA
+library:
+
+* ``Batch``: one plan (and one CUDA graph per direction) that transforms every
+  component grid, replacing the per-grid ``hierarchize`` calls on
+  ``instances[i % n]`` (:164-174).
+* ``CombinationTechnique``: subspace enumeration and the FP64 combine
+  (:176-290), the restriction of the combined subspaces back onto each
+  component grid, and the scatter onto a full grid (:293-318).
+* ``combination_scheme``: the classical level sets |l|_1 = n - q with
+  coefficients (-1)^q * C(d-1, q).
+"""
+from __future__ import annotations
+
+import ctypes
+import itertools
+import math
+
+from . import _lib
+from .transform import _dtype_code, _stream_handle, wavelet_id
+
+
+def combination_scheme(ndim, level_sum, qmax=None, minimum_level=1):
+    """Classical combination technique: every level vector l with
+    l_i >= minimum_level and |l|_1 = level_sum - q for q = 0..qmax, with
+    coefficient (-1)^q * C(ndim - 1, q). Level vectors are listed in
+    q-major, then lexicographic order."""
+    if qmax is None:
+        qmax = ndim - 1
+    lmin = ([minimum_level] * ndim if isinstance(minimum_level, int)
+            else list(minimum_level))
+    levels, coeffs = [], []
+    for q in range(qmax + 1):
+        m = level_sum - q
+        for l in _compositions(m, lmin):
+            levels.append(tuple(l))
+            coeffs.append((-1) ** q * math.comb(ndim - 1, q))
+    return levels, coeffs
+
+
+def _compositions(total, lmin):
+    if len(lmin) == 1:
+        if total >= lmin[0]:
+            yield (total,)
+        return
+    rest_min = sum(lmin[1:])
+    for first in range(lmin[0], total - rest_min + 1):
+        for tail in _compositions(total - first, lmin[1:]):
+            yield (first,) + tail
+
+
+def packed_grids(levels, dtype, device="cuda", align=64):
+    """One device allocation holding every grid (each start aligned to
+    ``align`` elements); returns (buffer, list of flat views)."""
+    import torch
+    sizes = [1 << sum(int(x) for x in l) for l in levels]
+    offsets, off = [], 0
+    for s in sizes:
+        offsets.append(off)
+        off += (s + align - 1) // align * align
+    buf = torch.empty(off, dtype=dtype, device=device)
+    return buf, [buf.narrow(0, o, s) for o, s in zip(offsets, sizes)]
+
+
+def _ptr_array(grids):
+    arr = (ctypes.c_void_p * len(grids))()
+    for i, g in enumerate(grids):
+        arr[i] = g.data_ptr()
+    return arr
+
+
+def _check_grids(grids, levels):
+    if len(grids) != len(levels):
+        raise _lib.InvalidArgument("one level vector per grid")
+    dt = grids[0].dtype
+    for g, l in zip(grids, levels):
+        if not g.is_cuda or not g.is_contiguous() or g.dtype != dt:
+            raise _lib.InvalidArgument(
+                "grids must be contiguous CUDA tensors of one dtype")
+        if g.numel() != 1 << sum(int(x) for x in l):
+            raise _lib.InvalidArgument("grid size does not match its level")
+
+
+class Batch:
+    """Forward / inverse transform of many grids with one plan.
+
+    ``grids`` are CUDA tensors (bound by address at construction),
+    ``levels[i]`` the level vector of grid i; ``minimum_level`` and
+    ``maximum_level`` are shared, as in the reference's driver."""
+
+    def __init__(self, grids, levels, minimum_level, maximum_level,
+                 wavelet_name="hat", compensated=False):
+        _check_grids(grids, levels)
+        self.grids = list(grids)
+        self.levels = [tuple(int(x) for x in l) for l in levels]
+        ndim = len(self.levels[0])
+        flat = [x for l in self.levels for x in l]
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        _lib.check(self._lib.paliwa_gb_batch_create(
+            ndim, len(grids), _lib.i64(flat), _lib.i64(minimum_level),
+            _lib.i64(maximum_level), _dtype_code(grids[0], compensated),
+            wavelet_id(wavelet_name), _ptr_array(grids),
+            ctypes.byref(self._h)))
+        self.points = sum(g.numel() for g in grids)
+
+    def hierarchize(self, stream=None):
+        _lib.check(self._lib.paliwa_gb_batch_hierarchize(
+            self._h, _stream_handle(self.grids[0], stream)))
+
+    def dehierarchize(self, stream=None):
+        _lib.check(self._lib.paliwa_gb_batch_dehierarchize(
+            self._h, _stream_handle(self.grids[0], stream)))
+
+    def use_graphs(self, enable):
+        _lib.check(self._lib.paliwa_gb_batch_use_graphs(self._h, int(enable)))
+
+    def launches(self):
+        p, f, i = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(self._lib.paliwa_gb_batch_info(
+            self._h, ctypes.byref(p), ctypes.byref(f), ctypes.byref(i)))
+        return f.value, i.value
+
+    def profile(self, forward=True, stream=None):
+        """Per-launch (milliseconds, algorithmic bytes) of one direction,
+        launched without a graph and bracketed by CUDA events."""
+        n = ctypes.c_int()
+        s = _stream_handle(self.grids[0], stream)
+        _lib.check(self._lib.paliwa_gb_batch_profile(
+            self._h, int(forward), s, 0, ctypes.byref(n), None, None))
+        ms = (ctypes.c_float * max(1, n.value))()
+        by = (ctypes.c_int64 * max(1, n.value))()
+        _lib.check(self._lib.paliwa_gb_batch_profile(
+            self._h, int(forward), s, n.value, ctypes.byref(n), ms, by))
+        return list(ms[:n.value]), list(by[:n.value])
+
+    def close(self):
+        if self._h:
+            self._lib.paliwa_gb_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CombinationTechnique:
+    """Sparse-grid combine / restrict / scatter of a combination scheme."""
+
+    def __init__(self, grids, levels, coefficients, maximum_level,
+                 keep_all=False):
+        _check_grids(grids, levels)
+        self.grids = list(grids)
+        self.levels = [tuple(int(x) for x in l) for l in levels]
+        self.maximum_level = tuple(int(x) for x in maximum_level)
+        self.ndim = len(self.levels[0])
+        flat = [x for l in self.levels for x in l]
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        dtype = _lib.F64 if grids[0].dtype.itemsize == 8 else _lib.F32
+        _lib.check(self._lib.paliwa_gb_ct_create(
+            self.ndim, len(grids), _lib.i64(flat), _lib.f64(coefficients),
+            _lib.i64(self.maximum_level), dtype, _ptr_array(grids),
+            int(keep_all), ctypes.byref(self._h)))
+        n, ns = ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(self._lib.paliwa_gb_ct_info(self._h, ctypes.byref(n),
+                                               ctypes.byref(ns)))
+        self.npoints, self.nsubspaces = n.value, ns.value
+
+    def subspaces(self):
+        """(level vectors, first sparse point of each), lexicographic."""
+        lv = (ctypes.c_int64 * max(1, self.nsubspaces * self.ndim))()
+        off = (ctypes.c_int64 * max(1, self.nsubspaces))()
+        _lib.check(self._lib.paliwa_gb_ct_subspaces(self._h, lv, off))
+        levels = [tuple(lv[i * self.ndim:(i + 1) * self.ndim])
+                  for i in range(self.nsubspaces)]
+        return levels, list(off[:self.nsubspaces])
+
+    def combine(self, sparse=None, stream=None):
+        import torch
+        if sparse is None:
+            sparse = torch.empty(self.npoints, dtype=torch.float64,
+                                 device=self.grids[0].device)
+        self._check_sparse(sparse)
+        _lib.check(self._lib.paliwa_gb_ct_combine(
+            self._h, sparse.data_ptr(), _stream_handle(self.grids[0], stream)))
+        return sparse
+
+    def restrict(self, sparse, stream=None):
+        self._check_sparse(sparse)
+        _lib.check(self._lib.paliwa_gb_ct_restrict(
+            self._h, sparse.data_ptr(), _stream_handle(self.grids[0], stream)))
+
+    def scatter(self, sparse, full=None, stream=None):
+        import torch
+        self._check_sparse(sparse)
+        shape = [1 << l for l in self.maximum_level]
+        if full is None:
+            full = torch.empty(shape, dtype=torch.float64,
+                               device=self.grids[0].device)
+        if (full.dtype != torch.float64 or not full.is_contiguous()
+                or full.numel() != math.prod(shape)):
+            raise _lib.InvalidArgument("full grid must be float64 at lmax")
+        _lib.check(self._lib.paliwa_gb_ct_scatter(
+            self._h, sparse.data_ptr(), full.data_ptr(),
+            _stream_handle(self.grids[0], stream)))
+        return full
+
+    def _check_sparse(self, sparse):
+        import torch
+        if (sparse.dtype != torch.float64 or not sparse.is_cuda
+                or not sparse.is_contiguous()
+                or sparse.numel() != self.npoints):
+            raise _lib.InvalidArgument(
+                f"sparse grid must be a float64 CUDA tensor of {self.npoints}")
+
+    def close(self):
+        if self._h:
+            self._lib.paliwa_gb_ct_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def subspace_count(levels):
+    """Host restatement of the subspace counting, for planning and tests
+    (paliwa_utils.hpp:9-26)."""
+    counts = {}
+    for lv in levels:
+        for s in itertools.product(*[range(int(x) + 1) for x in lv]):
+            counts[s] = counts.get(s, 0) + 1
+    return counts

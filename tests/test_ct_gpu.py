@@ -1,0 +1,192 @@
+"""Batched transforms and the combination technique on the GPU, against the
+oracle restatement of the reference's test driver
+(test/test_paliwa_combination_technique.cpp)."""
+import math
+
+import numpy as np
+import pytest
+
+import paliwa_gb300 as pg
+from paliwa_gb300 import ct as pct
+
+pytestmark = pytest.mark.gpu
+
+# test/test_paliwa_combination_technique.cpp:84-125
+SCHEMES = {
+    2: dict(lmax=(10, 11), lmin=(2, 3),
+            levels=[(2, 11), (3, 10), (4, 9), (5, 8), (6, 7), (7, 6), (8, 5),
+                    (9, 4), (10, 3), (2, 10), (3, 9), (4, 8), (5, 7), (6, 6),
+                    (7, 5), (8, 4), (9, 3)],
+            coeffs=[1] * 9 + [-1] * 8, full=106496, sparse=18432),
+    3: dict(lmax=(5, 6, 7), lmin=(4, 5, 6),
+            levels=[(4, 6, 7), (5, 5, 7), (5, 6, 6), (4, 5, 6)],
+            coeffs=[1, 1, 1, -2], full=425984, sparse=131072),
+    4: dict(lmax=(3, 4, 5, 6), lmin=(1, 2, 3, 4),
+            levels=[(2, 2, 4, 4), (3, 2, 3, 4), (1, 4, 3, 4), (1, 2, 5, 4),
+                    (2, 3, 3, 4), (1, 3, 4, 4), (2, 2, 3, 5), (1, 3, 3, 5),
+                    (1, 2, 3, 6), (1, 2, 4, 5), (1, 2, 4, 4), (2, 2, 3, 4),
+                    (1, 3, 3, 4), (1, 2, 3, 5), (1, 2, 3, 4)],
+            coeffs=[1] * 10 + [-3] * 4 + [3], full=50176, sparse=5120),
+}
+
+
+def oracle():
+    import oracle as o
+    o.build()
+    return o
+
+
+def sine_grid(level, lmax):
+    """prod_i sin(pi x_i) at x = uid / 2^L (:61-71 with
+    paliwa_dimensions.hpp:71-79)."""
+    f = None
+    for d, (l, L) in enumerate(zip(level, lmax)):
+        x = (np.arange(1 << l) << (L - l)) / float(1 << L)
+        shape = [1] * len(level)
+        shape[d] = len(x)
+        v = np.sin(math.pi * x).reshape(shape)
+        f = v if f is None else f * v
+    return np.ascontiguousarray(np.broadcast_to(f, [1 << l for l in level]))
+
+
+def upload(arrays):
+    import torch
+    return [torch.from_numpy(a.copy()).cuda().reshape(-1) for a in arrays]
+
+
+@pytest.mark.parametrize("d", [2, 3, 4])
+@pytest.mark.parametrize("wavelet", ["hat", "biorthogonal", "fullweighting"])
+def test_batch_matches_oracle_per_grid(d, wavelet):
+    sc = SCHEMES[d]
+    rng = np.random.default_rng(d)
+    xs = [rng.uniform(-1, 1, [1 << l for l in lv]) for lv in sc["levels"]]
+    gs = upload(xs)
+    b = pct.Batch(gs, sc["levels"], sc["lmin"], sc["lmax"], wavelet)
+    import torch
+    b.hierarchize(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    O = oracle()
+    for g, x, lv in zip(gs, xs, sc["levels"]):
+        want = O.hierarchize(x.copy(), lv, sc["lmin"], sc["lmax"], wavelet)
+        assert np.array_equal(g.cpu().numpy().reshape(want.shape), want)
+    b.dehierarchize()  # legacy default stream: direct launches
+    torch.cuda.synchronize()
+    for g, x in zip(gs, xs):
+        assert np.max(np.abs(g.cpu().numpy().reshape(x.shape) - x)) <= 1e-13
+    b.close()
+
+
+def test_batch_graph_replay_and_compensated():
+    import torch
+    sc = SCHEMES[4]
+    rng = np.random.default_rng(5)
+    xs = [rng.uniform(-1, 1, [1 << l for l in lv]) for lv in sc["levels"]]
+    O = oracle()
+    wants = [O.hierarchize(x.copy(), lv, sc["lmin"], sc["lmax"], "biorthogonal")
+             for x, lv in zip(xs, sc["levels"])]
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        g32 = [t.float() for t in upload(xs)]
+        b = pct.Batch(g32, sc["levels"], sc["lmin"], sc["lmax"],
+                      "biorthogonal", compensated=True)
+        for rep in range(3):  # capture once, replay; inverse in between
+            b.hierarchize(s)
+            s.synchronize()
+            for g, w in zip(g32, wants):
+                got = g.double().cpu().numpy().reshape(w.shape)
+                assert np.max(np.abs(got - w)) / np.max(np.abs(w)) <= 1e-6
+            b.dehierarchize(s)
+        b.close()
+
+
+def test_long_pencils_in_batch():
+    """Grids whose pencils exceed one CTA mix windowed and sub-lattice stages
+    with ordinary jobs in one plan."""
+    import torch
+    levels = [(17, 1), (1, 16), (13, 4), (9, 8), (2, 2)]
+    lmin, lmax = (1, 1), (17, 16)
+    rng = np.random.default_rng(1)
+    xs = [rng.uniform(-1, 1, [1 << l for l in lv]) for lv in levels]
+    buf, gs = pct.packed_grids(levels, torch.float64)
+    for g, x in zip(gs, xs):
+        g.copy_(torch.from_numpy(x.reshape(-1)))
+    b = pct.Batch(gs, levels, lmin, lmax, "biorthogonal")
+    s = torch.cuda.Stream()
+    b.hierarchize(s)
+    s.synchronize()
+    O = oracle()
+    for g, x, lv in zip(gs, xs, levels):
+        want = O.hierarchize(x.copy(), lv, lmin, lmax, "biorthogonal")
+        assert np.array_equal(g.cpu().numpy().reshape(want.shape), want)
+
+
+@pytest.mark.parametrize("d", [2, 3, 4])
+def test_combination_technique_reference_driver(d):
+    """The reference driver end to end (:77-340): sizes, FP64 combine
+    (bit-exact against the oracle restatement), scatter, full-grid
+    dehierarchize and the integral check mean ~ (2/pi)^d within 0.031."""
+    import torch
+    sc = SCHEMES[d]
+    O = oracle()
+    xs = [sine_grid(lv, sc["lmax"]) for lv in sc["levels"]]
+    assert sum(x.size for x in xs) == sc["full"]
+    gs = upload(xs)
+    b = pct.Batch(gs, sc["levels"], sc["lmin"], sc["lmax"], "biorthogonal")
+    b.hierarchize()
+    ct = pct.CombinationTechnique(gs, sc["levels"], sc["coeffs"], sc["lmax"])
+    assert ct.npoints == sc["sparse"]
+    subs, offs = ct.subspaces()
+    assert subs == O.kept_subspaces(sc["levels"])
+    sparse = ct.combine()
+    torch.cuda.synchronize()
+    hier = [O.hierarchize(x.copy(), lv, sc["lmin"], sc["lmax"], "biorthogonal")
+            for x, lv in zip(xs, sc["levels"])]
+    want = O.combine(hier, sc["levels"], sc["coeffs"], sc["lmax"], subs)
+    got = sparse.cpu().numpy()
+    for w, off in zip(want, offs):
+        assert np.array_equal(got[off:off + w.size], w.reshape(-1))
+    full = ct.scatter(sparse)
+    torch.cuda.synchronize()
+    want_full = O.scatter(want, subs, sc["lmax"])
+    assert np.array_equal(full.cpu().numpy(), want_full)
+    pg.dehierarchize(full, sc["lmax"], sc["lmin"], sc["lmax"], "biorthogonal")
+    mean = float(full.mean())
+    assert abs(mean - (2 / math.pi) ** d) <= 0.031
+    O.dehierarchize(want_full, sc["lmax"], sc["lmin"], sc["lmax"],
+                    "biorthogonal")
+    assert np.array_equal(full.cpu().numpy(), want_full)
+    ct.close()
+
+
+def test_restrict_writes_combined_values():
+    import torch
+    sc = SCHEMES[2]
+    rng = np.random.default_rng(3)
+    xs = [rng.uniform(-1, 1, [1 << l for l in lv]) for lv in sc["levels"]]
+    gs = upload(xs)
+    ct = pct.CombinationTechnique(gs, sc["levels"], sc["coeffs"], sc["lmax"])
+    sparse = ct.combine()
+    ct.restrict(sparse)
+    torch.cuda.synchronize()
+    O = oracle()
+    subs, offs = ct.subspaces()
+    sp = sparse.cpu().numpy()
+    for g, lv, x in zip(gs, sc["levels"], xs):
+        arr = g.cpu().numpy().reshape(x.shape)
+        written = np.zeros(x.shape, bool)
+        for s, off in zip(subs, offs):
+            if any(si > li for si, li in zip(s, lv)):
+                continue
+            sl = O.subspace_slices(s, lv)
+            n = O.subspace_size(s)
+            assert np.array_equal(arr[sl].reshape(-1), sp[off:off + n])
+            written[sl] = True
+        assert np.array_equal(arr[~written], x[~written])
+
+
+def test_classical_scheme_sizes():
+    levels, coeffs = pct.combination_scheme(4, 20, 3, 1)
+    counts = [sum(1 for l in levels if sum(l) == 20 - q) for q in range(4)]
+    assert counts == [969, 816, 680, 560]
+    assert sum(1 << sum(l) for l in levels) == 1695547392
+    assert set(coeffs) == {1, -3, 3, -1}

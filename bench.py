@@ -3,23 +3,35 @@
 python bench.py [--gpus N --steps K --warmup W] [--workload NAME]
                 [--impl reference]
 
+Workloads (seeded synthetic inputs; the reference publishes no dataset):
+  4d-ct-20  (default) batched 4D combination technique: every level vector
+            l >= 1 with |l|_1 = 20 - q, q = 0..3 (969 + 816 + 680 + 560 =
+            3025 periodic component grids, 1,695,547,392 points), CDF (2,2)
+            lifting ("biorthogonal", the wavelet of the reference's own CT
+            driver), f(x) = prod_i 4 x_i (1 - x_i) exp(-a_i x_i), a_i ~ U[0,2].
+  6d-ct-16  batched 6D CT, |l|_1 = 16 - q, q = 0..5 (7798 grids), sum of 4
+            anisotropic Gaussians plus N(0, 1e-4) noise.
+  3d-biorthogonal-999  one 512^3 grid, 8 Gaussians plus N(0, 1e-3) noise.
+  6d-hat-555544        one 32^4 x 16^2 grid, product of cosines + noise.
+
 A step is one full forward (hierarchize) plus one full inverse
-(dehierarchize) of the workload's grid(s), so the data stays bounded across
-repetitions. ``value`` is grid points transformed per second by the
-FP32-compensated path (2 * points per step), with the inputs resident in HBM;
-the same workload in plain FP64 is timed beside it (``fp64``), and the FP32c
-error against FP64 is reported. ``e2e`` repeats the FP32c step through the
-public API with pinned host buffers, host<->device copies inside the timed
-region. ``roofline`` is the per-axis lifting kernel: algorithmic bytes per
-launch (one read and one write of the grid) over its CUDA-event duration.
+(dehierarchize) of every grid of the workload, so the data stays bounded
+across repetitions; inputs are far larger than the 129 MB L2. ``value`` is
+grid points transformed per second (2 x points per step) by the
+FP32-compensated path with the data resident in HBM; the plain FP64 path is
+timed on the same workload (``fp64``), and the FP32c forward result is
+compared with the FP64 one (normwise max / rms error, overall and per q).
+``e2e`` repeats the FP32c step through the public API with pinned host
+buffers and the host<->device copies inside the timed region. ``roofline``
+is the dominant lifting launch: algorithmic bytes (one read and one write of
+each grid point it stores) over its CUDA-event duration, from an event-
+bracketed pass over the same plan. ``--impl reference`` times the
+reference's CPU algorithm (the oracle port in oracle/; the reference itself
+needs DDC and Kokkos, which are absent) on all host cores.
 
-``--impl reference`` times the reference's CPU algorithm (the oracle port in
-oracle/; the reference itself needs DDC and Kokkos, which are absent) on all
-host cores, for the same metric and workload.
-
-For N > 1 (torchrun), each rank runs an independent replica of the workload
-("replicas only": a single grid's transform does not shard without a ghost
-exchange); value sums the ranks' points over the slowest rank's time.
+For N > 1 (torchrun), each rank transforms an independent replica of the
+workload ("replicas only"); value sums the ranks' points over the slowest
+rank's time.
 """
 from __future__ import annotations
 
@@ -37,48 +49,98 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SEED_BASE = 20261203
+METRIC = ("points/s & % HBM roofline: batched FP32-comp vs plain FP64 at "
+          "stated error")
 
 WORKLOADS = {
-    # 3D CDF (2,2) lifting at levels (9,9,9): 512^3 periodic points, sum of
-    # 8 Gaussians (centres U[0,1]^3, widths U[0.02,0.2], amplitudes U[-1,1])
-    # plus N(0, 1e-3) noise.
-    "3d-biorthogonal-999": dict(level=(9, 9, 9), lmin=(0, 0, 0),
+    "4d-ct-20": dict(kind="ct", ndim=4, level_sum=20, qmax=3, lmin=1,
+                     wavelet="biorthogonal", config_id=4),
+    "6d-ct-16": dict(kind="ct", ndim=6, level_sum=16, qmax=5, lmin=1,
+                     wavelet="biorthogonal", config_id=5),
+    "3d-biorthogonal-999": dict(kind="grid", level=(9, 9, 9), lmin=(0, 0, 0),
                                 wavelet="biorthogonal", config_id=2),
-    # 6D hat at levels (5,5,5,5,4,4): 32^4 * 16^2 points, product of
-    # cos(k_i pi x_i), k_i in {1..4}, plus U[-1e-3, 1e-3].
-    "6d-hat-555544": dict(level=(5, 5, 5, 5, 4, 4), lmin=(0,) * 6,
-                          wavelet="hat", config_id=3),
+    "6d-hat-555544": dict(kind="grid", level=(5, 5, 5, 5, 4, 4),
+                          lmin=(0,) * 6, wavelet="hat", config_id=3),
 }
-DEFAULT_WORKLOAD = "3d-biorthogonal-999"
+DEFAULT_WORKLOAD = "4d-ct-20"
 
 
-def make_input(spec, rng):
-    """Seeded synthetic input in float64 (numpy, on the host)."""
-    import numpy as np
-    level = spec["level"]
-    axes = [np.arange(1 << l) / float(1 << l) for l in level]
-    cid = spec["config_id"]
-    if cid == 2:
-        out = np.zeros([1 << l for l in level])
-        grids = np.meshgrid(*axes, indexing="ij", sparse=True)
-        for _ in range(8):
-            c = rng.uniform(0, 1, 3)
-            w = rng.uniform(0.02, 0.2)
-            a = rng.uniform(-1, 1)
-            out += a * np.exp(-sum((g - ci) ** 2 for g, ci in zip(grids, c))
-                              / (2 * w * w))
-        out += rng.normal(0, 1e-3, out.shape)
-        return out
-    if cid == 3:
-        ks = rng.integers(1, 5, len(level))
-        f = None
-        for d, (x, k) in enumerate(zip(axes, ks)):
-            shape = [1] * len(level)
-            shape[d] = len(x)
-            v = np.cos(k * np.pi * x).reshape(shape)
-            f = v if f is None else f * v
-        return f + rng.uniform(-1e-3, 1e-3, [1 << l for l in level])
-    raise ValueError(cid)
+# ---------------------------------------------------------------------------
+# workload description and seeded inputs
+
+
+class Workload:
+    def __init__(self, name):
+        spec = WORKLOADS[name]
+        self.name, self.spec = name, spec
+        self.wavelet = spec["wavelet"]
+        if spec["kind"] == "ct":
+            from paliwa_gb300 import ct as pct
+            self.levels, self.coeffs = pct.combination_scheme(
+                spec["ndim"], spec["level_sum"], spec["qmax"], spec["lmin"])
+            d = spec["ndim"]
+            self.lmin = (spec["lmin"],) * d
+            top = spec["level_sum"] - (d - 1) * spec["lmin"]
+            self.lmax = (top,) * d
+            self.q = [spec["level_sum"] - sum(l) for l in self.levels]
+        else:
+            self.levels = [tuple(spec["level"])]
+            self.coeffs = [1.0]
+            self.lmin = tuple(spec["lmin"])
+            self.lmax = tuple(spec["level"])
+            self.q = [0]
+        self.ndim = len(self.levels[0])
+        self.points = sum(1 << sum(l) for l in self.levels)
+        rng = __import__("numpy").random.default_rng(
+            SEED_BASE + spec["config_id"])
+        self._params(rng)
+
+    def _params(self, rng):
+        cid = self.spec["config_id"]
+        d = self.ndim
+        if cid == 4:
+            self.a = rng.uniform(0, 2, d)
+        elif cid == 5:
+            self.gauss = [(rng.uniform(0, 1, d), rng.uniform(0.05, 0.3, d),
+                           rng.uniform(-1, 1)) for _ in range(4)]
+            self.noise_seed = int(rng.integers(1 << 31))
+        elif cid == 2:
+            self.gauss = [(rng.uniform(0, 1, 3), rng.uniform(0.02, 0.2),
+                           rng.uniform(-1, 1)) for _ in range(8)]
+            self.noise_seed = int(rng.integers(1 << 31))
+        elif cid == 3:
+            self.ks = rng.integers(1, 5, d)
+            self.noise_seed = int(rng.integers(1 << 31))
+
+    def grid_values(self, i):
+        """float64 values of grid i on the host (numpy), x = k / 2^l."""
+        import numpy as np
+        lv = self.levels[i]
+        xs = [np.arange(1 << l) / float(1 << l) for l in lv]
+        shape = [1 << l for l in lv]
+        cid = self.spec["config_id"]
+
+        def outer(factors):
+            f = factors[0]
+            for g in factors[1:]:
+                f = np.multiply.outer(f, g)
+            return f
+
+        if cid == 4:
+            return outer([4 * x * (1 - x) * np.exp(-a * x)
+                          for x, a in zip(xs, self.a)])
+        if cid == 3:
+            return outer([np.cos(k * np.pi * x) for x, k in zip(xs, self.ks)]
+                         ) + np.random.default_rng(self.noise_seed).uniform(
+                             -1e-3, 1e-3, shape)
+        out = np.zeros(shape)
+        for c, w, amp in self.gauss:
+            w = np.broadcast_to(w, (len(lv),))
+            out += amp * outer([np.exp(-(x - ci) ** 2 / (2 * wi * wi))
+                                for x, ci, wi in zip(xs, c, w)])
+        sigma = 1e-4 if cid == 5 else 1e-3
+        seed = self.noise_seed + i
+        return out + np.random.default_rng(seed).normal(0, sigma, shape)
 
 
 # ---------------------------------------------------------------------------
@@ -93,9 +155,7 @@ class ClockSampler:
               "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
-        self.proc = None
-        self.lines = []
+        self.index, self.proc, self.lines = index, None, []
 
     def __enter__(self):
         try:
@@ -104,8 +164,7 @@ class ClockSampler:
                  f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "100"], stdout=subprocess.PIPE,
                 stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except FileNotFoundError:
             self.proc = None
         return self
@@ -143,20 +202,19 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-# ---------------------------------------------------------------------------
-
-
 def peaks():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        with open(path) as f:
-            p = json.load(f)
-        return float(p["hbm_gbs"]), "measured"
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
 
 
-def dist_setup(args):
+# ---------------------------------------------------------------------------
+# multi-rank plumbing (replicas)
+
+
+def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -181,235 +239,281 @@ def max_over_ranks(world, value):
         return value
     import torch
     import torch.distributed as dist
-    dev = "cuda" if torch.cuda.is_available() and \
-        dist.get_backend() == "nccl" else "cpu"
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
     t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
 
-def run_reference(args, spec, world, rank):
-    """CPU reference arm: the oracle port of paliwa's algorithm (packed-pole
-    execution, the reference's fastest CPU mode) on all host cores."""
+def config_of(w, args):
+    c = {"workload": w.name, "grids": len(w.levels), "points": w.points,
+         "ndim": w.ndim, "minimum_level": list(w.lmin),
+         "maximum_level": list(w.lmax), "wavelet": w.wavelet,
+         "step": "hierarchize + dehierarchize of every grid",
+         "l2": "inputs larger than L2 (no flush needed)"}
+    if w.spec["kind"] == "ct":
+        c["level_sum"] = w.spec["level_sum"]
+        c["q"] = list(range(w.spec["qmax"] + 1))
+    else:
+        c["level"] = list(w.levels[0])
+    return c
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle port of the reference algorithm
+
+
+def cpu_transform_all(w, arrays, oracle):
+    t0 = time.perf_counter()
+    for x, lv in zip(arrays, w.levels):
+        oracle.hierarchize(x, lv, w.lmin, w.lmax, w.wavelet, mode=1)
+    for x, lv in zip(arrays, w.levels):
+        oracle.dehierarchize(x, lv, w.lmin, w.lmax, w.wavelet, mode=1)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, w, world, rank):
     if rank != 0:
         return
-    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
     cores = oracle.max_threads()
-    rng = np.random.default_rng(SEED_BASE + spec["config_id"])
-    x = make_input(spec, rng)
-    level, lmin = spec["level"], spec["lmin"]
-    npts = x.size
-
-    def step():
-        oracle.hierarchize(x, level, lmin, level, spec["wavelet"], mode=1)
-        oracle.dehierarchize(x, level, lmin, level, spec["wavelet"], mode=1)
-
+    arrays = [w.grid_values(i) for i in range(len(w.levels))]
     for _ in range(args.warmup):
-        step()
-    t0 = time.perf_counter()
+        cpu_transform_all(w, arrays, oracle)
+    dt = 0.0
     for _ in range(args.steps):
-        step()
-    dt = time.perf_counter() - t0
-    value = 2 * npts * args.steps / dt
+        dt += cpu_transform_all(w, arrays, oracle)
+    value = 2 * w.points * args.steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value,
         "unit": "points/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
-        "config": config_of(args, spec),
-        "cpu_baseline": {"value": value, "unit": "points/s", "cores": cores,
-                         "kind": "port",
-                         "sample": f"full workload grid ({npts} points), "
-                                   "forward + inverse per step, FP64, "
-                                   "packed-pole mode, OpenMP"},
+        "dtype": "f64", "data": "synthetic", "config": config_of(w, args),
+        "cpu_baseline": {
+            "value": value, "unit": "points/s", "cores": cores,
+            "kind": "port",
+            "sample": "every grid of the workload, forward + inverse per "
+                      "step, FP64, packed-pole mode, OpenMP"},
         "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-METRIC = "points/s & % HBM roofline: batched FP32-comp vs plain FP64 at stated error"
+# ---------------------------------------------------------------------------
+# GPU
 
 
-def config_of(args, spec):
-    return {"workload": args.workload, "level": list(spec["level"]),
-            "lmin": list(spec["lmin"]), "wavelet": spec["wavelet"],
-            "points": 1 << sum(spec["level"]),
-            "step": "hierarchize + dehierarchize, all dimensions",
-            "l2": "inputs larger than L2 (no flush needed)"}
-
-
-def run_gpu(args, spec, world, rank, local):
+def upload_inputs(w, dev):
+    """Packed device buffers (float64 and float32) of every grid, and a
+    pristine float64 copy for accuracy checks."""
     import numpy as np
     import torch
+    from paliwa_gb300 import ct as pct
+    b64, v64 = pct.packed_grids(w.levels, torch.float64, dev)
+    for i, v in enumerate(v64):
+        v.copy_(torch.from_numpy(np.ascontiguousarray(
+            w.grid_values(i)).reshape(-1)))
+    b32, v32 = pct.packed_grids(w.levels, torch.float32, dev)
+    b32.copy_(b64)
+    return b64, v64, b32, v32
 
-    import paliwa_gb300 as pg
-    dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
-    level, lmin, wavelet = spec["level"], spec["lmin"], spec["wavelet"]
-    ndim = len(level)
-    rng = np.random.default_rng(SEED_BASE + spec["config_id"])
-    x64 = make_input(spec, rng)
-    npts = x64.size
-    stream = torch.cuda.current_stream(dev)
 
-    g64 = torch.from_numpy(x64).to(dev)
-    g32 = torch.from_numpy(x64.astype(np.float32)).to(dev)
-
-    # Accuracy of the compensated FP32 forward transform against FP64 (the
-    # GPU FP64 path is bit-identical to the CPU oracle; see tests).
-    pg.hierarchize(g64, level, lmin, level, wavelet)
-    pg.hierarchize(g32, level, lmin, level, wavelet, compensated=True)
-    diff = g32.double() - g64
-    ref_max = float(g64.abs().max())
-    err_max = float(diff.abs().max()) / ref_max
-    err_rms = float(diff.pow(2).mean().sqrt() / g64.pow(2).mean().sqrt())
-    del diff
-    g64.copy_(torch.from_numpy(x64))
-    g32.copy_(torch.from_numpy(x64.astype(np.float32)))
-
-    def one_step(g, comp, evs=None):
-        # per-axis calls so that each lift launch is bracketed by events
-        for d in range(ndim):
-            if evs is not None:
-                evs.append(torch.cuda.Event(enable_timing=True))
-                evs[-1].record(stream)
-            pg.hierarchize_in(g, d, level, lmin, level, wavelet,
-                              compensated=comp)
-        for d in range(ndim):
-            if evs is not None:
-                evs.append(torch.cuda.Event(enable_timing=True))
-                evs[-1].record(stream)
-            pg.dehierarchize_in(g, d, level, lmin, level, wavelet,
-                                compensated=comp)
-        if evs is not None:
-            evs.append(torch.cuda.Event(enable_timing=True))
-            evs[-1].record(stream)
-
-    def timed(g, comp):
-        for _ in range(args.warmup):
-            one_step(g, comp)
-        barrier(world)
-        torch.cuda.synchronize()
-        evs = []
-        start = torch.cuda.Event(enable_timing=True)
-        end = torch.cuda.Event(enable_timing=True)
-        start.record(stream)
-        for _ in range(args.steps):
-            one_step(g, comp, evs)
-        end.record(stream)
-        torch.cuda.synchronize()
-        barrier(world)
-        total_ms = start.elapsed_time(end)
-        launches = [evs[i].elapsed_time(evs[i + 1])
-                    for i in range(len(evs) - 1) if (i + 1) % (2 * ndim + 1)]
-        return total_ms, launches
-
-    with ClockSampler(local) as clocks:
-        ms32, launch32 = timed(g32, True)
-    ms64, launch64 = timed(g64, False)
-
-    ms32 = max_over_ranks(world, ms32)
-    ms64 = max_over_ranks(world, ms64)
-    pts_per_step = 2 * npts * world
-    value = pts_per_step * args.steps / (ms32 / 1e3)
-    value64 = pts_per_step * args.steps / (ms64 / 1e3)
-
-    peak, peak_kind = peaks()
-    bytes_launch32 = 2 * npts * 4
-    avg32 = sum(launch32) / len(launch32)
-    achieved = bytes_launch32 / (avg32 / 1e3) / 1e9
-    bytes_launch64 = 2 * npts * 8
-    avg64 = sum(launch64) / len(launch64)
-    achieved64 = bytes_launch64 / (avg64 / 1e3) / 1e9
-
-    # End to end through the public API: pinned host input, H2D, forward +
-    # inverse, D2H of the result, every step.
-    host_in = torch.from_numpy(x64.astype(np.float32)).pin_memory()
-    host_out = torch.empty_like(host_in).pin_memory()
-    ge = torch.empty(host_in.shape, dtype=torch.float32, device=dev)
-
-    def e2e_step():
-        ge.copy_(host_in, non_blocking=True)
-        pg.hierarchize(ge, level, lmin, level, wavelet, compensated=True)
-        pg.dehierarchize(ge, level, lmin, level, wavelet, compensated=True)
-        host_out.copy_(ge, non_blocking=True)
-
-    for _ in range(args.warmup):
-        e2e_step()
+def time_steps(fwd, inv, steps, warmup, stream, world):
+    import torch
+    for _ in range(warmup):
+        fwd()
+        inv()
     barrier(world)
     torch.cuda.synchronize()
     s = torch.cuda.Event(enable_timing=True)
     e = torch.cuda.Event(enable_timing=True)
     s.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
+    for _ in range(steps):
+        fwd()
+        inv()
     e.record(stream)
     torch.cuda.synchronize()
     barrier(world)
-    e2e_ms = max_over_ranks(world, s.elapsed_time(e))
-    e2e_value = pts_per_step * args.steps / (e2e_ms / 1e3)
+    return s.elapsed_time(e)
+
+
+def run_gpu(args, w, world, rank, local):
+    import numpy as np
+    import torch
+
+    import paliwa_gb300 as pg
+    from paliwa_gb300 import ct as pct
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(dev)
+    b64, v64, b32, v32 = upload_inputs(w, dev)
+    pristine = b64.clone()
+
+    with torch.cuda.stream(stream):
+        bt64 = pct.Batch(v64, w.levels, w.lmin, w.lmax, w.wavelet)
+        bt32 = pct.Batch(v32, w.levels, w.lmin, w.lmax, w.wavelet,
+                         compensated=True)
+        # Accuracy of the compensated FP32 forward transform against FP64.
+        bt64.hierarchize(stream)
+        bt32.hierarchize(stream)
+        stream.synchronize()
+        err = {"norm": "max|e|/max|ref| and rms(e)/rms(ref) over the grids"}
+        qs = sorted(set(w.q))
+        per_q = {}
+        off = 0
+        # grids are packed in q-major order: group contiguous ranges
+        bounds = {}
+        for i, (q, v) in enumerate(zip(w.q, v64)):
+            start = v.data_ptr() - b64.data_ptr()
+            bounds.setdefault(q, [start // 8, 0])
+            bounds[q][1] = start // 8 + v.numel()
+        tot_max = tot_ref = 0.0
+        tot_sq = tot_rsq = 0.0
+        for q in qs:
+            lo, hi = bounds[q]
+            r = b64[lo:hi]
+            e = b32[lo:hi].double() - r
+            emax, rmax = float(e.abs().max()), float(r.abs().max())
+            esq, rsq = float(e.pow(2).sum()), float(r.pow(2).sum())
+            per_q[str(q)] = {"max_rel": emax / rmax,
+                             "rms_rel": math.sqrt(esq / rsq)}
+            tot_max, tot_ref = max(tot_max, emax), max(tot_ref, rmax)
+            tot_sq, tot_rsq = tot_sq + esq, tot_rsq + rsq
+            del e
+        err["max_rel"] = tot_max / tot_ref
+        err["rms_rel"] = math.sqrt(tot_sq / tot_rsq)
+        if len(qs) > 1:
+            err["per_q"] = per_q
+        del off
+
+        # Combine / restrict in FP64 (sparse grid of the kept subspaces).
+        combine = None
+        if w.spec["kind"] == "ct":
+            ct = pct.CombinationTechnique(v32, w.levels, w.coeffs, w.lmax)
+            sparse = ct.combine()
+            ct.restrict(sparse)
+            stream.synchronize()
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s2 = torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            ct.combine(sparse)
+            s1.record(stream)
+            ct.restrict(sparse)
+            s2.record(stream)
+            stream.synchronize()
+            combine = {"sparse_points": ct.npoints,
+                       "subspaces": ct.nsubspaces,
+                       "combine_ms": s0.elapsed_time(s1),
+                       "restrict_ms": s1.elapsed_time(s2),
+                       "dtype": "f64 accumulation of f32 grids"}
+            ct.close()
+        b64.copy_(pristine)
+        b32.copy_(pristine)
+        del pristine
+
+        with ClockSampler(local) as clocks:
+            ms32 = time_steps(lambda: bt32.hierarchize(stream),
+                              lambda: bt32.dehierarchize(stream),
+                              args.steps, args.warmup, stream, world)
+        ms64 = time_steps(lambda: bt64.hierarchize(stream),
+                          lambda: bt64.dehierarchize(stream),
+                          args.steps, args.warmup, stream, world)
+        # Per-launch durations of the same plan, event-bracketed.
+        prof = {}
+        for name, bt in (("f32c", bt32), ("f64", bt64)):
+            rows = []
+            for fwd in (True, False):
+                ms, by = bt.profile(fwd, stream)
+                rows += list(zip(ms, by))
+            prof[name] = rows
+        nlaunch = sum(bt32.launches())
+
+    ms32 = max_over_ranks(world, ms32)
+    ms64 = max_over_ranks(world, ms64)
+    pts_step = 2 * w.points * world
+    value = pts_step * args.steps / (ms32 / 1e3)
+    value64 = pts_step * args.steps / (ms64 / 1e3)
+    peak, peak_kind = peaks()
+
+    def roof(rows):
+        top = max(rows, key=lambda r: r[0])
+        tot_ms = sum(r[0] for r in rows)
+        tot_b = sum(r[1] for r in rows)
+        return top, tot_ms, tot_b
+
+    top32, tot32_ms, tot32_b = roof(prof["f32c"])
+    top64, tot64_ms, tot64_b = roof(prof["f64"])
+    achieved = top32[1] / (top32[0] / 1e3) / 1e9
+
+    # End to end through the public API with pinned host buffers.
+    host_in = torch.empty(b32.numel(), dtype=torch.float32).pin_memory()
+    host_in.copy_(b32)
+    host_out = torch.empty_like(host_in).pin_memory()
+
+    def e2e_fwd():
+        b32.copy_(host_in, non_blocking=True)
+        bt32.hierarchize(stream)
+
+    def e2e_inv():
+        bt32.dehierarchize(stream)
+        host_out.copy_(b32, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        e2e_ms = time_steps(e2e_fwd, e2e_inv, max(1, args.steps // 2),
+                            args.warmup, stream, world)
+    e2e_ms = max_over_ranks(world, e2e_ms)
+    e2e_value = pts_step * max(1, args.steps // 2) / (e2e_ms / 1e3)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(spec, x64)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        arrays = [w.grid_values(i) for i in range(len(w.levels))]
+        dt = cpu_transform_all(w, arrays, oracle)
+        cpu = {"value": 2 * w.points / dt, "unit": "points/s",
+               "cores": oracle.max_threads(), "kind": "port",
+               "sample": "every grid of the workload once, forward + "
+                         "inverse, FP64, packed-pole mode, OpenMP"}
 
-    ksum = kernel_counts()
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "points/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms32 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32c",
-            "data": "synthetic", "config": config_of(args, spec),
+            "data": "synthetic", "config": config_of(w, args),
             "fp64": {"value": value64, "unit": "points/s",
                      "ms_per_step": ms64 / args.steps,
                      "speedup_f32c_over_f64": value / value64,
-                     "roofline_frac": achieved64 / peak},
-            "error_f32c_vs_f64": {"max_rel": err_max, "rms_rel": err_rms,
-                                  "norm": "max|e|/max|ref|, rms(e)/rms(ref)"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "peak_kind": peak_kind,
-                         "kernel": "lift_kernel (one axis, FP32c)",
-                         "bytes_per_launch": bytes_launch32,
-                         "avg_launch_ms": avg32},
+                     "hbm_frac_all_launches":
+                         tot64_b / (tot64_ms / 1e3) / 1e9 / peak},
+            "error_f32c_vs_f64": err,
+            "roofline": {
+                "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                "peak_kind": peak_kind,
+                "kernel": "lift_kernel<CompensatedSym> (largest launch)",
+                "bytes_per_launch": top32[1], "launch_ms": top32[0],
+                "all_launches_frac":
+                    tot32_b / (tot32_ms / 1e3) / 1e9 / peak},
+            "combine": combine,
             "clocks": clocks.summary(),
             "e2e": {"value": e2e_value, "unit": "points/s",
-                    "h2d_bytes_per_step": npts * 4,
-                    "d2h_bytes_per_step": npts * 4},
-            "gpu_launches": args.steps * 2 * ndim * ksum,
+                    "h2d_bytes_per_step": b32.numel() * 4,
+                    "d2h_bytes_per_step": b32.numel() * 4},
+            "gpu_launches": args.steps * nlaunch,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-
-
-def kernel_counts():
-    """Lift launches per axis pass of the workloads here (all pencils fit one
-    CTA: one launch per axis)."""
-    return 1
-
-
-def cpu_baseline(spec, x64):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
-    import oracle
-    oracle.build()
-    cores = oracle.max_threads()
-    level, lmin = spec["level"], spec["lmin"]
-    y = x64.copy()
-    t0 = time.perf_counter()
-    oracle.hierarchize(y, level, lmin, level, spec["wavelet"], mode=1)
-    oracle.dehierarchize(y, level, lmin, level, spec["wavelet"], mode=1)
-    dt = time.perf_counter() - t0
-    return {"value": 2 * y.size / dt, "unit": "points/s", "cores": cores,
-            "kind": "port",
-            "sample": f"one forward + inverse of the full grid ({y.size} "
-                      "points), FP64, packed-pole mode, OpenMP"}
+    bt32.close()
+    bt64.close()
 
 
 def main():
@@ -423,14 +527,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline leg")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
-    spec = WORKLOADS[args.workload]
-    world, rank, local = dist_setup(args)
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_setup()
+    w = Workload(args.workload)
     if args.impl == "reference":
-        run_reference(args, spec, world, rank)
+        run_reference(args, w, world, rank)
     else:
-        run_gpu(args, spec, world, rank, local)
+        run_gpu(args, w, world, rank, local)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -8,8 +8,12 @@
 
 namespace pgb {
 
+// One lifting pass's coefficients in both precisions, converted once on the
+// host: on GB300 a double->float conversion runs on the (slow) FP64 pipe, so
+// none may happen per update.
 struct Coeffs {
   double c0, c1, c2;
+  float f0, f1, f2;
 };
 
 // ---------------------------------------------------------------------------
@@ -32,16 +36,26 @@ template <typename T, bool ExactProducts> struct Plain {
 
   // C1: the middle coefficient is exactly 1 (skips one multiply).
   // F64: unused (plain arithmetic has a single precision).
+  static __device__ __forceinline__ T k0(Coeffs const &c) {
+    if constexpr (sizeof(T) == 8) return c.c0; else return c.f0;
+  }
+  static __device__ __forceinline__ T k1(Coeffs const &c) {
+    if constexpr (sizeof(T) == 8) return c.c1; else return c.f1;
+  }
+  static __device__ __forceinline__ T k2(Coeffs const &c) {
+    if constexpr (sizeof(T) == 8) return c.c2; else return c.f2;
+  }
+
   template <bool C1, bool F64>
   static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
                                              V up) {
     if constexpr (ExactProducts) {
-      V t = C1 ? me : mul(T(c.c1), me);
-      t = fma(T(c.c0), lo, t);
-      return fma(T(c.c2), up, t);
+      V t = C1 ? me : mul(k1(c), me);
+      t = fma(k0(c), lo, t);
+      return fma(k2(c), up, t);
     } else {
-      V t = add(mul(T(c.c0), lo), C1 ? me : mul(T(c.c1), me));
-      return add(t, mul(T(c.c2), up));
+      V t = add(mul(k0(c), lo), C1 ? me : mul(k1(c), me));
+      return add(t, mul(k2(c), up));
     }
   }
 
@@ -104,7 +118,12 @@ __device__ __forceinline__ DF df_scale(float c, DF a) {
   return {p, e};
 }
 
-struct Compensated {
+// Sym: every pass of the launch has c0 == c2 and only exact-scaler
+// coefficients (true for all of paliwa's wavelet tables). The update is then
+// evaluated as c1*me + c*(lo + up) with two TwoSums and exact scalings
+// (17 flops instead of 31); the pair is kept unnormalized, which TwoSum
+// tolerates, and is rounded to float once when stored.
+template <bool Sym> struct CompensatedT {
   using V = DF;
   using Store = float;
   static __device__ __forceinline__ V load(Store x) { return {x, 0.0f}; }
@@ -128,13 +147,25 @@ struct Compensated {
       double t = C1 ? m : __dmul_rn(c.c1, m);
       t = __fma_rn(c.c0, to_double(lo), t);
       return from_double(__fma_rn(c.c2, to_double(up), t));
+    } else if constexpr (Sym) {
+      float const cc = c.f0;
+      DF const s = two_sum(lo.h, up.h);
+      float const e1 = __fadd_rn(s.l, __fadd_rn(lo.l, up.l));
+      float const t = __fmul_rn(cc, s.h);
+      float const m = C1 ? me.h : __fmul_rn(c.f1, me.h);
+      DF const r = two_sum(m, t);
+      float l = __fmaf_rn(cc, e1, r.l);
+      l = C1 ? __fadd_rn(l, me.l) : __fmaf_rn(c.f1, me.l, l);
+      return {r.h, l};
     } else {
-      DF p0 = df_scale(float(c.c0), lo);
-      DF p1 = C1 ? me : df_scale(float(c.c1), me);
-      DF p2 = df_scale(float(c.c2), up);
+      DF p0 = df_scale(c.f0, lo);
+      DF p1 = C1 ? me : df_scale(c.f1, me);
+      DF p2 = df_scale(c.f2, up);
       return df_add(df_add(p0, p1), p2);
     }
   }
 };
+using Compensated = CompensatedT<false>;
+using CompensatedSym = CompensatedT<true>;
 
 } // namespace pgb

@@ -35,6 +35,7 @@ struct Launch {
 struct Direction {
   LiftParams params{};
   bool exact = true;
+  bool symmetric = true;
   std::vector<Launch> launches;
   LiftJob *jobs_dev = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -90,6 +91,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
   auto const filters = wavelet_filters(b.wavelet, forward);
   dr.params = launch_params(filters);
   dr.exact = exact_scalers(filters);
+  dr.symmetric = symmetric_filters(filters);
   std::vector<LiftJob> all_jobs;
   for (int d = 0; d < b.ndim; ++d) {
     // stages[g] = the ordered stages of grid g along axis d
@@ -135,8 +137,8 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
 void run_direction(paliwa_gb_batch &b, Direction &dr, cudaStream_t s) {
   auto launch_all = [&] {
     for (auto const &L : dr.launches)
-      launch_lift(b.dtype, dr.exact, L.R, dr.params, dr.jobs_dev + L.job_first,
-                  L.njobs, L.tiles, s);
+      launch_lift(b.dtype, dr.exact, dr.symmetric, L.R, dr.params,
+                  dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
   };
   cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
   if (s != nullptr)
@@ -400,7 +402,7 @@ int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
     cuda_check(cudaEventRecord(ev[0], s), "cudaEventRecord");
     for (int i = 0; i < n; ++i) {
       Launch const &L = dr.launches[i];
-      launch_lift(batch->dtype, dr.exact, L.R, dr.params,
+      launch_lift(batch->dtype, dr.exact, dr.symmetric, L.R, dr.params,
                   dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
       cuda_check(cudaEventRecord(ev[i + 1], s), "cudaEventRecord");
       bytes[i] = static_cast<int64_t>(2 * es) * L.points;

@@ -42,6 +42,12 @@ bool exact_scalers(std::vector<Filter> const &filters) {
   return true;
 }
 
+bool symmetric_filters(std::vector<Filter> const &filters) {
+  for (auto const &f : filters)
+    if (f.c[0] != f.c[2]) return false;
+  return true;
+}
+
 int chunk_for(int log2_n) {
   if (log2_n <= 4) return 1 << log2_n;  // whole pencil in one thread
   return 16;
@@ -99,7 +105,9 @@ LiftParams launch_params(std::vector<Filter> const &filters) {
     if (filters[i].offset != 0 && filters[i].offset != 1)
       throw StatusError(PALIWA_GB_RUNTIME_ERROR, "Filter offset not supported");
     p.offsets[i] = filters[i].offset;
-    p.coeffs[i] = {filters[i].c[0], filters[i].c[1], filters[i].c[2]};
+    p.coeffs[i] = {filters[i].c[0],        filters[i].c[1],
+                   filters[i].c[2],        float(filters[i].c[0]),
+                   float(filters[i].c[1]), float(filters[i].c[2])};
     if (filters[i].c[1] == 1.0) p.c1_one_mask |= 1u << i;
   }
   return p;
@@ -269,9 +277,9 @@ void launch_a(int R, LiftParams const &p, cudaStream_t s) {
 
 } // namespace
 
-void launch_lift(int dtype, bool exact, int R, LiftParams params,
-                 LiftJob const *jobs, int njobs, long long total_tiles,
-                 cudaStream_t s) {
+void launch_lift(int dtype, bool exact, bool symmetric, int R,
+                 LiftParams params, LiftJob const *jobs, int njobs,
+                 long long total_tiles, cudaStream_t s) {
   if (total_tiles <= 0 || R < 2) return;
   params.jobs = jobs;
   params.njobs = njobs;
@@ -285,6 +293,7 @@ void launch_lift(int dtype, bool exact, int R, LiftParams params,
     if (exact) return launch_a<Plain<float, true>>(R, params, s);
     return launch_a<Plain<float, false>>(R, params, s);
   case PALIWA_GB_F32C:
+    if (exact && symmetric) return launch_a<CompensatedSym>(R, params, s);
     return launch_a<Compensated>(R, params, s);
   }
   throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
@@ -327,10 +336,11 @@ void transform_axis(void *grid, int dtype, int ndim, int64_t const *level,
                       dim),
             shifts, filters, stages);
   bool const exact = exact_scalers(filters);
+  bool const sym = symmetric_filters(filters);
   for (auto const &st : stages) {
     LiftParams p = params;
     p.job = st.job;
-    launch_lift(dtype, exact, st.R, p, nullptr, 1, st.tiles, s);
+    launch_lift(dtype, exact, sym, st.R, p, nullptr, 1, st.tiles, s);
   }
 }
 

@@ -325,14 +325,30 @@ __global__ void __launch_bounds__(NT)
 
   int const t = threadIdx.x;
   int const lane = t & 31;
+  // The current job lives in shared memory: its fields are read in the inner
+  // loops, and a generic pointer into parameter or global space would turn
+  // every read into a memory instruction.
+  __shared__ LiftJob sjob;
+  __shared__ int sjob_index;
+  LiftJob const *const job = &sjob;
   int ji = 0;
-  LiftJob const *job = p.jobs != nullptr ? p.jobs : &p.job;
+  if (t == 0) sjob_index = -1;
   // Persistent CTAs: tiles are visited in increasing order, so the job
   // cursor only moves forward.
   for (long long tile = blockIdx.x; tile < p.total_tiles; tile += gridDim.x) {
-    if (p.jobs != nullptr) {
+    if (p.jobs != nullptr)
       while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
-      job = p.jobs + ji;
+    __syncthreads();  // the previous tile is out of shared memory
+    if (sjob_index != ji) {
+      __syncthreads();  // every thread has read sjob_index
+      constexpr int WORDS = sizeof(LiftJob) / 4;
+      static_assert(sizeof(LiftJob) % 4 == 0, "LiftJob is copied in words");
+      unsigned const *src = reinterpret_cast<unsigned const *>(
+          p.jobs != nullptr ? p.jobs + ji : &p.job);
+      for (int i = t; i < WORDS; i += NT)
+        reinterpret_cast<unsigned *>(&sjob)[i] = src[i];
+      if (t == 0) sjob_index = ji;
+      __syncthreads();
     }
     int const log2W = job->log2_window;       // points per column held
     int const log2G = log2W - LOG2R;          // chunks per column
@@ -352,7 +368,6 @@ __global__ void __launch_bounds__(NT)
 
     unsigned char *const gbase = reinterpret_cast<unsigned char *>(job->base);
 
-    __syncthreads();  // the previous tile is out of shared memory
     // ---- load: global -> stage
     TileCopy<S, R, NT> cp(*job, periodic, log2W, cols, gc0, wstart, n, pitch,
                           gbase);

@@ -32,6 +32,8 @@ struct Filter {
 // Wavelet tables, paliwa/paliwa_wavelets.hpp:15-28.
 std::vector<Filter> wavelet_filters(int wavelet, bool forward);
 bool exact_scalers(std::vector<Filter> const &filters);
+// Every pass has c0 == c2 (the symmetric lifting steps of all wavelets).
+bool symmetric_filters(std::vector<Filter> const &filters);
 
 // A dense view of the pencils along one axis.
 struct AxisView {
@@ -69,9 +71,9 @@ LiftParams launch_params(std::vector<Filter> const &filters);
 
 // Launch the lifting kernel for `dtype` over `njobs` jobs (device array
 // `jobs`, or the inline job of `params` when jobs == nullptr).
-void launch_lift(int dtype, bool exact, int R, LiftParams params,
-                 LiftJob const *jobs, int njobs, long long total_tiles,
-                 cudaStream_t stream);
+void launch_lift(int dtype, bool exact, bool symmetric, int R,
+                 LiftParams params, LiftJob const *jobs, int njobs,
+                 long long total_tiles, cudaStream_t stream);
 
 void cuda_check(cudaError_t e, char const *what);
 size_t dtype_size(int dtype);

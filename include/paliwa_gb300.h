@@ -48,8 +48,8 @@ enum {
   PALIWA_GB_F64 = 0,
   /* float storage, float arithmetic: the reference's Value = float. */
   PALIWA_GB_F32 = 1,
-  /* float storage, compensated (double-float) arithmetic in registers,
-   * rounded to float once per dimension; coarsest levels in FP64. */
+  /* float storage, compensated (double-float, 48-bit significand)
+   * arithmetic in registers, rounded to float once per dimension. */
   PALIWA_GB_F32C = 2
 };
 

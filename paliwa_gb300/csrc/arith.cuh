@@ -87,9 +87,10 @@ template <typename T, bool ExactProducts> struct Plain {
 // with l = 0. Each update evaluates c0*lo + c1*me + c2*up with error-free
 // transformations (FMA-based TwoProd, Knuth TwoSum), so rounding errors do not
 // accumulate along the level chain; the pair is rounded to one float only
-// when it is stored, i.e. once per dimension. The coarsest levels (at most a
-// few points per pencil) are evaluated in FP64, as the mass-conservation
-// property of those steps is the most sensitive to rounding.
+// when it is stored, i.e. once per dimension. An FP64 mode for the coarsest
+// levels exists (LiftParams::fp64_log2_points) but is off by default: on
+// GB300 those per-pencil steps occupy the FP64 pipe for whole warp
+// instructions with one to four active lanes.
 struct DF {
   float h, l;
 };

@@ -100,7 +100,11 @@ LiftParams launch_params(std::vector<Filter> const &filters) {
   LiftParams p;
   std::memset(&p, 0, sizeof(p));
   p.npasses = static_cast<int>(filters.size());
-  p.fp64_log2_points = 2;
+  // Per-pencil FP64 steps run as whole warp instructions on GB300's FP64
+  // pipe even when only one lane is active; measured, they cost more than
+  // the rest of the FP32-compensated transform. The coarsest levels
+  // therefore stay in double-float arithmetic unless enabled here.
+  p.fp64_log2_points = -1;
   for (size_t i = 0; i < filters.size(); ++i) {
     if (filters[i].offset != 0 && filters[i].offset != 1)
       throw StatusError(PALIWA_GB_RUNTIME_ERROR, "Filter offset not supported");

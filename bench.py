@@ -353,6 +353,8 @@ def run_gpu(args, w, world, rank, local):
     stream = torch.cuda.Stream(dev)
     b64, v64, b32, v32 = upload_inputs(w, dev)
     pristine = b64.clone()
+    # The uploads ran on the default stream; order the work stream after them.
+    torch.cuda.synchronize()
 
     with torch.cuda.stream(stream):
         bt64 = pct.Batch(v64, w.levels, w.lmin, w.lmax, w.wavelet)
@@ -415,6 +417,7 @@ def run_gpu(args, w, world, rank, local):
             ct.close()
         b64.copy_(pristine)
         b32.copy_(pristine)
+        stream.synchronize()
         del pristine
 
         with ClockSampler(local) as clocks:

@@ -177,3 +177,51 @@ def import_oracle():
     import oracle
     oracle.build()
     return oracle
+
+
+CT_SHAPES = [(17, 1, 1, 1), (1, 17, 1, 1), (1, 1, 17, 1), (1, 1, 1, 17),
+             (12, 2, 3, 3), (3, 12, 2, 3), (2, 3, 12, 3), (5, 5, 5, 5),
+             (1, 1, 9, 9), (14, 1, 2, 3)]
+
+
+@pytest.mark.parametrize("level", CT_SHAPES)
+def test_ct_shapes_f64_exact_and_f32c_error(level):
+    """Component-grid shapes of the 4D combination technique (|l|_1 = 17..20,
+    l >= 1), lmin = 1: FP64 bit-exact, FP32c within 1e-6 of FP64, single grid
+    and in one batch."""
+    from paliwa_gb300 import ct as pct
+    lmin = (1, 1, 1, 1)
+    lmax = (17, 17, 17, 17)
+    x = random_input(level, 31)
+    O = import_oracle()
+    for forward in (True, False):
+        want = O.hierarchize(x.copy(), level, lmin, lmax, "biorthogonal",
+                             forward=forward)
+        got = gpu_transform(x, level, lmin, lmax, "biorthogonal", forward)
+        assert np.array_equal(got, want)
+        got32 = gpu_transform(x.astype(np.float32), level, lmin, lmax,
+                              "biorthogonal", forward, compensated=True)
+        err = np.max(np.abs(got32 - want)) / np.max(np.abs(want))
+        assert err <= F32C_TOL, (level, forward, err)
+
+
+def test_ct_shapes_in_one_batch_f32c():
+    import torch
+    from paliwa_gb300 import ct as pct
+    lmin, lmax = (1, 1, 1, 1), (17, 17, 17, 17)
+    xs = [random_input(l, i) for i, l in enumerate(CT_SHAPES)]
+    O = import_oracle()
+    wants = [O.hierarchize(x.copy(), l, lmin, lmax, "biorthogonal")
+             for x, l in zip(xs, CT_SHAPES)]
+    buf, gs = pct.packed_grids(CT_SHAPES, torch.float32)
+    for g, x in zip(gs, xs):
+        g.copy_(torch.from_numpy(x.astype(np.float32).reshape(-1)))
+    torch.cuda.synchronize()
+    b = pct.Batch(gs, CT_SHAPES, lmin, lmax, "biorthogonal", compensated=True)
+    s = torch.cuda.Stream()
+    b.hierarchize(s)
+    s.synchronize()
+    for g, w, l in zip(gs, wants, CT_SHAPES):
+        got = g.double().cpu().numpy().reshape(w.shape)
+        err = np.max(np.abs(got - w)) / np.max(np.abs(w))
+        assert err <= F32C_TOL, (l, err)

@@ -81,6 +81,10 @@ struct paliwa_gb_batch {
   long long points = 0;
   bool use_graphs = true;
   Direction dir[2];  // 0 = forward, 1 = inverse
+  // Shadow buffers of the windowed stages (grids with pencils longer than
+  // one CTA holds), reused by every axis: one direction runs at a time.
+  void *shadow = nullptr;
+  size_t shadow_bytes = 0;
 };
 
 namespace {
@@ -93,15 +97,27 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
   dr.exact = exact_scalers(filters);
   dr.symmetric = symmetric_filters(filters);
   std::vector<LiftJob> all_jobs;
+  size_t const es = dtype_size(b.dtype);
   for (int d = 0; d < b.ndim; ++d) {
     // stages[g] = the ordered stages of grid g along axis d
     std::vector<std::vector<Stage>> stages(b.ngrids);
     size_t depth = 0;
+    size_t shadow_off = 0;
     for (int g = 0; g < b.ngrids; ++g) {
       int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
-      plan_axis(axis_view(reinterpret_cast<unsigned long long>(grid_ptrs[g]),
-                          b.ndim, lv, d),
-                level_shifts(lv[d], lmin[d], forward), filters, stages[g]);
+      AxisView view = axis_view(
+          reinterpret_cast<unsigned long long>(grid_ptrs[g]), b.ndim, lv, d);
+      auto const shifts = level_shifts(lv[d], lmin[d], forward);
+      if (needs_shadow(view, shifts)) {
+        size_t bytes = es;
+        for (int k = 0; k < b.ndim; ++k) bytes <<= lv[k];
+        if (shadow_off + bytes > b.shadow_bytes)
+          throw StatusError(PALIWA_GB_RUNTIME_ERROR, "shadow plan overflow");
+        view.shadow =
+            reinterpret_cast<unsigned long long>(b.shadow) + shadow_off;
+        shadow_off += (bytes + 255) / 256 * 256;
+      }
+      plan_axis(view, shifts, filters, stages[g]);
       depth = std::max(depth, stages[g].size());
     }
     for (size_t k = 0; k < depth; ++k) {
@@ -335,12 +351,29 @@ int paliwa_gb_batch_create(int ndim, int ngrids, const int64_t *levels,
       for (int d = 0; d < ndim; ++d) total += levels[g * ndim + d];
       b->points += 1LL << total;
     }
+    // Shadow space: the largest per-axis total over the grids whose pencils
+    // along that axis need windowed stages.
+    for (int d = 0; d < ndim; ++d) {
+      size_t total = 0;
+      for (int g = 0; g < ngrids; ++g) {
+        int64_t const *lv = levels + static_cast<size_t>(g) * ndim;
+        if (lv[d] <= kWindowLog2 || lv[d] == minimum_level[d]) continue;
+        size_t bytes = es;
+        for (int k = 0; k < ndim; ++k) bytes <<= lv[k];
+        total += (bytes + 255) / 256 * 256;
+      }
+      b->shadow_bytes = std::max(b->shadow_bytes, total);
+    }
     try {
+      if (b->shadow_bytes)
+        cuda_check(cudaMalloc(&b->shadow, b->shadow_bytes),
+                   "cudaMalloc(shadow)");
       plan_direction(*b, b->dir[0], true, levels, minimum_level, grid_ptrs);
       plan_direction(*b, b->dir[1], false, levels, minimum_level, grid_ptrs);
     } catch (...) {
       free_direction(b->dir[0]);
       free_direction(b->dir[1]);
+      if (b->shadow) cudaFree(b->shadow);
       throw;
     }
     *out = b.release();
@@ -419,6 +452,7 @@ void paliwa_gb_batch_destroy(paliwa_gb_batch *batch) {
   if (batch == nullptr) return;
   free_direction(batch->dir[0]);
   free_direction(batch->dir[1]);
+  if (batch->shadow) cudaFree(batch->shadow);
   delete batch;
 }
 

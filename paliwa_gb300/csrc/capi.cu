@@ -126,6 +126,7 @@ LiftJob make_job(AxisView const &v, std::vector<int> const &sh, size_t first,
   LiftJob job;
   std::memset(&job, 0, sizeof(job));
   job.base = v.base;
+  job.dst_base = v.base;
   job.columns = v.columns;
   job.tile_begin = 0;
   job.log2_inner = v.log2_inner;
@@ -186,9 +187,16 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
     if (seg_len <= 0)
       throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
                         "filter list too long for windowed long pencils");
+    if (v.shadow == 0)
+      throw StatusError(PALIWA_GB_RUNTIME_ERROR,
+                        "windowed stage planned without a shadow buffer");
+    // Windows overlap their neighbours' segments, so they read the grid and
+    // store to the shadow; a copy stage (a window job without levels and
+    // without halo) then moves the shadow back into the grid.
     Stage st;
     st.R = R;
     st.job = make_job(v, shifts, first, count);
+    st.job.dst_base = v.shadow;
     st.job.periodic = 0;
     st.job.log2_window = kWindowLog2;
     st.job.seg_len = static_cast<int>(seg_len);
@@ -196,6 +204,18 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
     st.job.col_tiles = ceil_div(v.columns, C);
     st.tiles = ceil_div(1LL << v.log2_n, seg_len) * st.job.col_tiles;
     out.push_back(st);
+    Stage cp;
+    cp.R = R;
+    cp.job = make_job(v, shifts, first, 0);
+    cp.job.base = v.shadow;
+    cp.job.dst_base = v.base;
+    cp.job.periodic = 0;
+    cp.job.log2_window = kWindowLog2;
+    cp.job.seg_len = static_cast<int>(window);
+    cp.job.halo = 0;
+    cp.job.col_tiles = ceil_div(v.columns, C);
+    cp.tiles = ceil_div(1LL << v.log2_n, window) * cp.job.col_tiles;
+    out.push_back(cp);
     first += count;
   }
 }
@@ -335,17 +355,31 @@ void transform_axis(void *grid, int dtype, int ndim, int64_t const *level,
                     int dim, std::vector<int> const &shifts,
                     std::vector<Filter> const &filters, cudaStream_t s) {
   LiftParams const params = launch_params(filters);
-  std::vector<Stage> stages;
-  plan_axis(axis_view(reinterpret_cast<unsigned long long>(grid), ndim, level,
-                      dim),
-            shifts, filters, stages);
-  bool const exact = exact_scalers(filters);
-  bool const sym = symmetric_filters(filters);
-  for (auto const &st : stages) {
-    LiftParams p = params;
-    p.job = st.job;
-    launch_lift(dtype, exact, sym, st.R, p, nullptr, 1, st.tiles, s);
+  AxisView view =
+      axis_view(reinterpret_cast<unsigned long long>(grid), ndim, level, dim);
+  void *shadow = nullptr;
+  if (needs_shadow(view, shifts)) {
+    // Stream-ordered scratch for the windowed stages of long pencils.
+    size_t bytes = dtype_size(dtype);
+    for (int d = 0; d < ndim; ++d) bytes <<= level[d];
+    cuda_check(cudaMallocAsync(&shadow, bytes, s), "cudaMallocAsync(shadow)");
+    view.shadow = reinterpret_cast<unsigned long long>(shadow);
   }
+  try {
+    std::vector<Stage> stages;
+    plan_axis(view, shifts, filters, stages);
+    bool const exact = exact_scalers(filters);
+    bool const sym = symmetric_filters(filters);
+    for (auto const &st : stages) {
+      LiftParams p = params;
+      p.job = st.job;
+      launch_lift(dtype, exact, sym, st.R, p, nullptr, 1, st.tiles, s);
+    }
+  } catch (...) {
+    if (shadow) cudaFreeAsync(shadow, s);
+    throw;
+  }
+  if (shadow) cuda_check(cudaFreeAsync(shadow, s), "cudaFreeAsync(shadow)");
 }
 
 void check_levels(int ndim, int64_t const *level, int64_t const *lmin,

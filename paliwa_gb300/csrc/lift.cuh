@@ -38,6 +38,10 @@ constexpr int kMaxLevels = 48;
 // along one axis. Jobs of a launch are sorted by tile_begin.
 struct LiftJob {
   unsigned long long base;  // byte address of the grid's first element
+  // Byte address the results are stored to (same layout). Equal to `base`
+  // for in-place stages; windowed stages store to a shadow buffer, because
+  // their halos overlap the neighbouring windows' stored segments.
+  unsigned long long dst_base;
   long long columns;        // outer * inner
   long long tile_begin;     // index of the first tile of this job
   long long col_tiles;      // tiles per window row (ceil(columns / C))
@@ -219,9 +223,10 @@ template <typename S, int R, int NT> struct TileCopy {
                                       int halo, int seg_len) const {
     int const log2B = job.log2_inner;
     int const log2cols = 31 - __clz(cols);
-    S *const g = reinterpret_cast<S *>(gbase);
+    S *const g = reinterpret_cast<S *>(
+        Store ? reinterpret_cast<unsigned char *>(job.dst_base) : gbase);
     long long const columns = job.columns;
-    bool const aligned = (job.base & 15ull) == 0;
+    bool const aligned = ((job.base | job.dst_base) & 15ull) == 0;
     int const log2RL = log2B < log2cols ? log2B : log2cols;
     if (aligned && VEC > 1 && (1 << log2RL) >= VEC) {
       // rows of RL contiguous elements; row rho = (a_off, k)

@@ -38,6 +38,9 @@ bool symmetric_filters(std::vector<Filter> const &filters);
 // A dense view of the pencils along one axis.
 struct AxisView {
   unsigned long long base = 0;  // byte address of the grid
+  // Byte address of a buffer with the grid's size and layout, used by the
+  // windowed stages of pencils longer than one CTA holds (0: none).
+  unsigned long long shadow = 0;
   long long columns = 1;        // outer * inner
   int log2_inner = 0;
   int log2_kstride = 0;  // element stride between consecutive pencil points
@@ -65,6 +68,11 @@ constexpr int kHaloBudget = 256;  // halo per side of a window, in points
 int chunk_for(int log2_n);        // R for a periodic pencil of 2^log2_n
 void plan_axis(AxisView const &view, std::vector<int> const &shifts,
                std::vector<Filter> const &filters, std::vector<Stage> &out);
+
+// True when planning `view` along `shifts` needs a shadow buffer.
+inline bool needs_shadow(AxisView const &view, std::vector<int> const &shifts) {
+  return !shifts.empty() && view.log2_n > kWindowLog2;
+}
 
 // Kernel-level parameters shared by every job of a launch.
 LiftParams launch_params(std::vector<Filter> const &filters);

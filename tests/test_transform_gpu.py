@@ -225,3 +225,20 @@ def test_ct_shapes_in_one_batch_f32c():
         got = g.double().cpu().numpy().reshape(w.shape)
         err = np.max(np.abs(got - w)) / np.max(np.abs(w))
         assert err <= F32C_TOL, (l, err)
+
+
+@pytest.mark.parametrize("level", [(18, 4), (3, 17, 2)])
+def test_long_pencils_many_tiles(level):
+    """Grids large enough that persistent CTAs process many windows each."""
+    lmin = (0,) * len(level)
+    x = random_input(level, 12)
+    O = import_oracle()
+    for forward in (True, False):
+        want = O.hierarchize(x.copy(), level, lmin, level, "biorthogonal",
+                             forward=forward)
+        got = gpu_transform(x, level, lmin, level, "biorthogonal", forward)
+        assert np.array_equal(got, want), (level, forward)
+        got32 = gpu_transform(x.astype(np.float32), level, lmin, level,
+                              "biorthogonal", forward, compensated=True)
+        err = np.max(np.abs(got32 - want)) / np.max(np.abs(want))
+        assert err <= F32C_TOL

@@ -26,6 +26,7 @@ namespace {
 
 struct Launch {
   int R = 0;
+  int sched = -1;
   size_t job_first = 0;  // index into the device job array
   int njobs = 0;
   long long tiles = 0;
@@ -128,6 +129,10 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
       for (auto const &[R, list] : by_r) {
         Launch L;
         L.R = R;
+        int const ws = wavelet_schedule(filters);
+        L.sched = ws;
+        for (Stage const *st : list)
+          if (ws < 0 || !canonical_shifts(st->job, (ws & 1) != 0)) L.sched = -1;
         L.job_first = all_jobs.size();
         L.njobs = static_cast<int>(list.size());
         for (Stage const *st : list) {
@@ -153,7 +158,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
 void run_direction(paliwa_gb_batch &b, Direction &dr, cudaStream_t s) {
   auto launch_all = [&] {
     for (auto const &L : dr.launches)
-      launch_lift(b.dtype, dr.exact, dr.symmetric, L.R, dr.params,
+      launch_lift(b.dtype, dr.exact, dr.symmetric, L.sched, L.R, dr.params,
                   dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
   };
   cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
@@ -435,8 +440,8 @@ int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
     cuda_check(cudaEventRecord(ev[0], s), "cudaEventRecord");
     for (int i = 0; i < n; ++i) {
       Launch const &L = dr.launches[i];
-      launch_lift(batch->dtype, dr.exact, dr.symmetric, L.R, dr.params,
-                  dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
+      launch_lift(batch->dtype, dr.exact, dr.symmetric, L.sched, L.R,
+                  dr.params, dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
       cuda_check(cudaEventRecord(ev[i + 1], s), "cudaEventRecord");
       bytes[i] = static_cast<int64_t>(2 * es) * L.points;
     }

@@ -6,7 +6,7 @@
 #include <vector>
 
 #include "paliwa_gb300.h"
-#include "plan.hpp"
+#include "launch.cuh"
 
 namespace pgb {
 
@@ -255,8 +255,6 @@ void plan_axis(AxisView const &view, std::vector<int> const &shifts,
   }
 }
 
-namespace {
-
 int device_sms() {
   int dev = 0, sms = 0;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -265,43 +263,27 @@ int device_sms() {
   return sms;
 }
 
-template <class A, int R>
-void launch_r(LiftParams const &p, cudaStream_t s) {
-  auto kernel = lift_kernel<A, R, kThreads>;
-  size_t const smem = lift_smem_bytes<A, R, kThreads>(kRounds);
-  static thread_local int per_sm = 0;
-  static thread_local int sms = 0;
-  if (per_sm == 0) {
-    cuda_check(cudaFuncSetAttribute(kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)),
-               "cudaFuncSetAttribute");
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &per_sm, kernel, kThreads, smem),
-               "occupancy query");
-    sms = device_sms();
-    if (per_sm < 1) per_sm = 1;
-  }
-  long long const resident = static_cast<long long>(per_sm) * sms;
-  long long const blocks = std::min(p.total_tiles, resident);
-  kernel<<<static_cast<unsigned>(blocks), kThreads, smem, s>>>(p);
-  cuda_check(cudaGetLastError(), "lift_kernel launch");
+int wavelet_schedule(std::vector<Filter> const &filters) {
+  for (int w = 0; w < 3; ++w)
+    for (int fwd = 0; fwd < 2; ++fwd) {
+      auto const t = wavelet_filters(w, fwd != 0);
+      if (t.size() != filters.size()) continue;
+      bool same = true;
+      for (size_t i = 0; i < t.size() && same; ++i)
+        same = t[i].offset == filters[i].offset && t[i].c[0] == filters[i].c[0] &&
+               t[i].c[1] == filters[i].c[1] && t[i].c[2] == filters[i].c[2];
+      if (same) return 2 * w + fwd;
+    }
+  return -1;
 }
 
-template <class A>
-void launch_a(int R, LiftParams const &p, cudaStream_t s) {
-  switch (R) {
-  case 2: return launch_r<A, 2>(p, s);
-  case 4: return launch_r<A, 4>(p, s);
-  case 8: return launch_r<A, 8>(p, s);
-  case 16: return launch_r<A, 16>(p, s);
-  }
-  throw StatusError(PALIWA_GB_RUNTIME_ERROR, "bad chunk size");
+bool canonical_shifts(LiftJob const &job, bool forward) {
+  for (int i = 0; i < job.nlevels; ++i)
+    if (job.shift[i] != (forward ? i : job.nlevels - 1 - i)) return false;
+  return true;
 }
 
-} // namespace
-
-void launch_lift(int dtype, bool exact, bool symmetric, int R,
+void launch_lift(int dtype, bool exact, bool symmetric, int sched, int R,
                  LiftParams params, LiftJob const *jobs, int njobs,
                  long long total_tiles, cudaStream_t s) {
   if (total_tiles <= 0 || R < 2) return;
@@ -309,16 +291,12 @@ void launch_lift(int dtype, bool exact, bool symmetric, int R,
   params.njobs = njobs;
   params.total_tiles = total_tiles;
   params.rounds = kRounds;
+  if (params.fp64_log2_points >= 0) sched = -1;
   switch (dtype) {
-  case PALIWA_GB_F64:
-    if (exact) return launch_a<Plain<double, true>>(R, params, s);
-    return launch_a<Plain<double, false>>(R, params, s);
-  case PALIWA_GB_F32:
-    if (exact) return launch_a<Plain<float, true>>(R, params, s);
-    return launch_a<Plain<float, false>>(R, params, s);
+  case PALIWA_GB_F64: return launch_lift_f64(exact, sched, R, params, s);
+  case PALIWA_GB_F32: return launch_lift_f32(exact, sched, R, params, s);
   case PALIWA_GB_F32C:
-    if (exact && symmetric) return launch_a<CompensatedSym>(R, params, s);
-    return launch_a<Compensated>(R, params, s);
+    return launch_lift_f32c(exact && symmetric, sched, R, params, s);
   }
   throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
 }
@@ -370,10 +348,13 @@ void transform_axis(void *grid, int dtype, int ndim, int64_t const *level,
     plan_axis(view, shifts, filters, stages);
     bool const exact = exact_scalers(filters);
     bool const sym = symmetric_filters(filters);
+    int const ws = wavelet_schedule(filters);
     for (auto const &st : stages) {
       LiftParams p = params;
       p.job = st.job;
-      launch_lift(dtype, exact, sym, st.R, p, nullptr, 1, st.tiles, s);
+      int const sched =
+          ws >= 0 && canonical_shifts(st.job, (ws & 1) != 0) ? ws : -1;
+      launch_lift(dtype, exact, sym, sched, st.R, p, nullptr, 1, st.tiles, s);
     }
   } catch (...) {
     if (shadow) cudaFreeAsync(shadow, s);

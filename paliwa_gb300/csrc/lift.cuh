@@ -173,6 +173,235 @@ __device__ __forceinline__ int stage_pitch(int G) {
   return (G * (R + 1)) | 1;
 }
 
+// Exchanges between the chunks of one column during the level steps of a
+// round. Chunk c of a column is lane c of its group when G <= 32 (warp
+// shuffles); longer columns exchange through shared memory with one barrier
+// per step (the same for every thread of the CTA: G is uniform per tile).
+template <class A, int NT> struct RoundCtx {
+  using V = typename A::V;
+  int t, c, G, log2G, gbase_lane, periodic;
+  V *heads, *xch;
+  int buf = 0;
+  bool heads_valid = false;
+
+  __device__ __forceinline__ RoundCtx(int t_, int c_, int G_, int log2G_,
+                                      int lane, int periodic_, V *heads_,
+                                      V *xch_)
+      : t(t_), c(c_), G(G_), log2G(log2G_), gbase_lane(lane & ~(G_ - 1)),
+        periodic(periodic_), heads(heads_), xch(xch_) {}
+
+  // The neighbour of a fine step: slot 0 of the next chunk (o = 1) or slot
+  // R - s of the previous chunk (o = 0); `pub` is this chunk's value of it.
+  __device__ __forceinline__ V fine_neighbor(int o, V pub) {
+    if (G == 1) return pub;
+    int nc = (o == 1) ? c + 1 : c - 1;
+    if (G <= 32) return shfl(pub, gbase_lane | (nc & (G - 1)));
+    xch[buf * NT + t] = pub;
+    __syncthreads();
+    if (periodic)
+      nc &= G - 1;
+    else
+      nc = nc < 0 ? 0 : (nc >= G ? G - 1 : nc);
+    V const r = xch[buf * NT + ((t >> log2G) << log2G) + nc];
+    buf ^= 1;
+    return r;
+  }
+  __device__ __forceinline__ void fine_wrote_heads(int o) {
+    if (o == 0) heads_valid = false;  // slot 0 changed
+  }
+
+  // One coarse step (distance d chunks) on the chunk heads.
+  template <class Upd>
+  __device__ __forceinline__ void coarse(V &v0, int o, int d, Upd upd) {
+    bool const mine = (c & (2 * d - 1)) == o * d;
+    if (G <= 32) {
+      V const lo = shfl(v0, gbase_lane | ((c - d) & (G - 1)));
+      V const up = shfl(v0, gbase_lane | ((c + d) & (G - 1)));
+      if (mine) v0 = upd(lo, v0, up);
+      return;
+    }
+    if (!heads_valid) {
+      heads[t] = v0;
+      __syncthreads();
+      heads_valid = true;
+    }
+    if (mine) {
+      int cl = c - d, cu = c + d;
+      if (periodic) {
+        cl &= G - 1;
+        cu &= G - 1;
+      } else {
+        cl = cl < 0 ? c : cl;
+        cu = cu >= G ? c : cu;
+      }
+      int const colbase = (t >> log2G) << log2G;
+      v0 = upd(heads[colbase + cl], v0, heads[colbase + cu]);
+      heads[t] = v0;
+    }
+    __syncthreads();
+  }
+};
+
+// Schedule for arbitrary level lists and filters (transform_in): levels,
+// parities and coefficients are read per step.
+struct RuntimeSched {
+  template <class A, int R, int NT>
+  static __device__ __forceinline__ void run(typename A::V (&v)[R],
+                                             RoundCtx<A, NT> &ctx,
+                                             LiftJob const &job,
+                                             LiftParams const &p) {
+    using V = typename A::V;
+    constexpr int LOG2R = Log2<R>::value;
+    int const nlev = job.nlevels;
+    for (int li = 0; li < nlev; ++li) {
+      int const sh = job.shift[li];
+      bool const f64 = (job.log2_n - sh - 1) <= p.fp64_log2_points;
+      for (int ps = 0; ps < p.npasses; ++ps) {
+        int const o = p.offsets[ps];
+        Coeffs const cf = p.coeffs[ps];
+        bool const c1one = (p.c1_one_mask >> ps) & 1u;
+        if (sh < LOG2R) {
+          V const pub = (o == 1) ? v[0] : tail_value<R>(v, sh);
+          V const nb = ctx.fine_neighbor(o, pub);
+          fine_dispatch<A, R>(v, sh, o, nb, cf, c1one, f64);
+          ctx.fine_wrote_heads(o);
+        } else {
+          ctx.coarse(v[0], o, 1 << (sh - LOG2R), [&](V lo, V me, V up) {
+            return coarse_update<A>(cf, c1one, f64, lo, me, up);
+          });
+        }
+      }
+    }
+  }
+};
+
+// Wavelet tables at compile time (paliwa/paliwa_wavelets.hpp:15-28).
+template <int O, int C0N, int C1N, int C2N, int DEN> struct Pass {
+  static constexpr int offset = O;
+  static constexpr bool c1one = C1N == DEN;
+  static __device__ __forceinline__ constexpr Coeffs coeffs() {
+    return {double(C0N) / DEN, double(C1N) / DEN, double(C2N) / DEN,
+            float(C0N) / DEN,  float(C1N) / DEN,  float(C2N) / DEN};
+  }
+};
+template <class... P> struct PassList {
+  static constexpr int size = sizeof...(P);
+};
+template <int W, bool FWD> struct WaveletPasses;
+// hat: forward {(1, {-1/2, 1, -1/2})}, inverse {(1, {1/2, 1, 1/2})}
+template <> struct WaveletPasses<0, true> {
+  using type = PassList<Pass<1, -2, 4, -2, 4>>;
+};
+template <> struct WaveletPasses<0, false> {
+  using type = PassList<Pass<1, 2, 4, 2, 4>>;
+};
+// biorthogonal: forward {(1, {-1/2, 1, -1/2}), (0, {1/4, 1, 1/4})},
+// inverse {(0, {-1/4, 1, -1/4}), (1, {1/2, 1, 1/2})}
+template <> struct WaveletPasses<1, true> {
+  using type = PassList<Pass<1, -2, 4, -2, 4>, Pass<0, 1, 4, 1, 4>>;
+};
+template <> struct WaveletPasses<1, false> {
+  using type = PassList<Pass<0, -1, 4, -1, 4>, Pass<1, 2, 4, 2, 4>>;
+};
+// fullweighting: forward {(0, {1/4, 1/2, 1/4}), (1, {-1/2, 1, -1/2})},
+// inverse {(1, {1/2, 1, 1/2}), (0, {-1/2, 2, -1/2})}
+template <> struct WaveletPasses<2, true> {
+  using type = PassList<Pass<0, 1, 2, 1, 4>, Pass<1, -2, 4, -2, 4>>;
+};
+template <> struct WaveletPasses<2, false> {
+  using type = PassList<Pass<1, 2, 4, 2, 4>, Pass<0, -2, 8, -2, 4>>;
+};
+
+// Schedule of hierarchize (FWD: levels fine to coarse, distances 1, 2, 4, ...)
+// and dehierarchize (coarse to fine) with a compile-time wavelet: the fine
+// levels are unrolled with compile-time distance, parity and coefficients.
+// The job's shifts are 0 .. L-1 (FWD) or L-1 .. 0.
+template <int W, bool FWD> struct WaveletSched {
+  using Passes = typename WaveletPasses<W, FWD>::type;
+
+  template <class A, int R, int NT, int K, class P>
+  static __device__ __forceinline__ void fine_pass(typename A::V (&v)[R],
+                                                   RoundCtx<A, NT> &ctx) {
+    using V = typename A::V;
+    constexpr int S = 1 << K;
+    constexpr Coeffs cf = P::coeffs();
+    V const pub = P::offset == 1 ? v[0] : v[R - S];
+    V const nb = ctx.fine_neighbor(P::offset, pub);
+    if constexpr (P::offset == 1) {
+#pragma unroll
+      for (int j = S; j < R; j += 2 * S) {
+        V const up = (j + S < R) ? v[(j + S) % R] : nb;
+        v[j] = A::template update<P::c1one, false>(cf, v[j - S], v[j], up);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < R; j += 2 * S) {
+        V const lo = (j >= S) ? v[(j + R - S) % R] : nb;
+        v[j] = A::template update<P::c1one, false>(cf, lo, v[j], v[j + S]);
+      }
+    }
+    ctx.fine_wrote_heads(P::offset);
+  }
+
+  template <class A, int R, int NT, int K, class... P>
+  static __device__ __forceinline__ void fine_level(typename A::V (&v)[R],
+                                                    RoundCtx<A, NT> &ctx,
+                                                    PassList<P...>) {
+    (fine_pass<A, R, NT, K, P>(v, ctx), ...);
+  }
+
+  template <class A, int R, int NT, class... P>
+  static __device__ __forceinline__ void coarse_level(typename A::V (&v)[R],
+                                                      RoundCtx<A, NT> &ctx,
+                                                      int d, PassList<P...>) {
+    using V = typename A::V;
+    (ctx.coarse(v[0], P::offset, d,
+                [](V lo, V me, V up) {
+                  constexpr Coeffs cf = P::coeffs();
+                  return A::template update<P::c1one, false>(cf, lo, me, up);
+                }),
+     ...);
+  }
+
+  template <class A, int R, int NT, int K>
+  static __device__ __forceinline__ void fine_up(typename A::V (&v)[R],
+                                                 RoundCtx<A, NT> &ctx, int L) {
+    if constexpr ((1 << K) < R) {
+      if (K < L) {
+        fine_level<A, R, NT, K>(v, ctx, Passes{});
+        fine_up<A, R, NT, K + 1>(v, ctx, L);
+      }
+    }
+  }
+  template <class A, int R, int NT, int K>
+  static __device__ __forceinline__ void fine_down(typename A::V (&v)[R],
+                                                   RoundCtx<A, NT> &ctx,
+                                                   int L) {
+    if constexpr (K >= 0) {
+      if (K < L) fine_level<A, R, NT, K>(v, ctx, Passes{});
+      fine_down<A, R, NT, K - 1>(v, ctx, L);
+    }
+  }
+
+  template <class A, int R, int NT>
+  static __device__ __forceinline__ void run(typename A::V (&v)[R],
+                                             RoundCtx<A, NT> &ctx,
+                                             LiftJob const &job,
+                                             LiftParams const &) {
+    constexpr int LOG2R = Log2<R>::value;
+    int const L = job.nlevels;
+    if constexpr (FWD) {
+      fine_up<A, R, NT, 0>(v, ctx, L);
+      for (int sh = LOG2R; sh < L; ++sh)
+        coarse_level<A, R, NT>(v, ctx, 1 << (sh - LOG2R), Passes{});
+    } else {
+      for (int sh = L - 1; sh >= LOG2R; --sh)
+        coarse_level<A, R, NT>(v, ctx, 1 << (sh - LOG2R), Passes{});
+      fine_down<A, R, NT, LOG2R - 1>(v, ctx, L);
+    }
+  }
+};
+
 // Copies one tile between global memory and the staging layout.
 //
 // The tile is `cols` consecutive columns (global column index gc0 + w) by
@@ -316,7 +545,7 @@ template <typename S, int R, int NT> struct TileCopy {
   }
 };
 
-template <class A, int R, int NT>
+template <class A, int R, int NT, class Sched>
 __global__ void __launch_bounds__(NT)
     lift_kernel(__grid_constant__ const LiftParams p) {
   using V = typename A::V;
@@ -387,73 +616,8 @@ __global__ void __launch_bounds__(NT)
       V v[R];
 #pragma unroll
       for (int j = 0; j < R; ++j) v[j] = A::load(chunk[j]);
-
-      // Lanes of one column inside a warp (G <= 32): shuffles only.
-      int const gbase_lane = lane & ~(G - 1);
-      bool heads_valid = false;
-      int buf = 0;
-      int const nlev = job->nlevels;
-      for (int li = 0; li < nlev; ++li) {
-        int const sh = job->shift[li];
-        bool const f64 = (job->log2_n - sh - 1) <= p.fp64_log2_points;
-        for (int ps = 0; ps < p.npasses; ++ps) {
-          int const o = p.offsets[ps];
-          Coeffs const cf = p.coeffs[ps];
-          bool const c1one = (p.c1_one_mask >> ps) & 1u;
-          if (sh < LOG2R) {
-            V nb;
-            V const pub = (o == 1) ? v[0] : tail_value<R>(v, sh);
-            if (G == 1) {
-              nb = pub;
-            } else if (G <= 32) {
-              int const nc = (o == 1) ? c + 1 : c - 1;
-              nb = shfl(pub, gbase_lane | (nc & (G - 1)));
-            } else {
-              xch[buf * NT + t] = pub;
-              __syncthreads();
-              int nc = (o == 1) ? c + 1 : c - 1;
-              if (periodic)
-                nc &= G - 1;
-              else
-                nc = nc < 0 ? 0 : (nc >= G ? G - 1 : nc);
-              nb = xch[buf * NT + ((t >> log2G) << log2G) + nc];
-              buf ^= 1;
-            }
-            fine_dispatch<A, R>(v, sh, o, nb, cf, c1one, f64);
-            if (o == 0) heads_valid = false;
-          } else {
-            int const d = 1 << (sh - LOG2R);
-            bool const mine = (c & (2 * d - 1)) == o * d;
-            if (G <= 32) {
-              V const lo = shfl(v[0], gbase_lane | ((c - d) & (G - 1)));
-              V const up = shfl(v[0], gbase_lane | ((c + d) & (G - 1)));
-              if (mine) v[0] = coarse_update<A>(cf, c1one, f64, lo, v[0], up);
-            } else {
-              if (!heads_valid) {
-                heads[t] = v[0];
-                __syncthreads();
-                heads_valid = true;
-              }
-              if (mine) {
-                int cl = c - d, cu = c + d;
-                if (periodic) {
-                  cl &= G - 1;
-                  cu &= G - 1;
-                } else {
-                  cl = cl < 0 ? c : cl;
-                  cu = cu >= G ? c : cu;
-                }
-                int const colbase = (t >> log2G) << log2G;
-                V const lo = heads[colbase + cl];
-                V const up = heads[colbase + cu];
-                v[0] = coarse_update<A>(cf, c1one, f64, lo, v[0], up);
-                heads[t] = v[0];
-              }
-              __syncthreads();
-            }
-          }
-        }
-      }
+      RoundCtx<A, NT> ctx(t, c, G, log2G, lane, periodic, heads, xch);
+      Sched::template run<A, R, NT>(v, ctx, *job, p);
 #pragma unroll
       for (int j = 0; j < R; ++j) chunk[j] = A::store(v[j]);
       if (G > 32) __syncthreads();  // heads / xch reused by the next round

@@ -79,9 +79,15 @@ LiftParams launch_params(std::vector<Filter> const &filters);
 
 // Launch the lifting kernel for `dtype` over `njobs` jobs (device array
 // `jobs`, or the inline job of `params` when jobs == nullptr).
-void launch_lift(int dtype, bool exact, bool symmetric, int R,
+// sched: 2 * wavelet + forward for the compile-time wavelet schedule (every
+// job's shifts must be canonical), or -1 for the runtime schedule.
+void launch_lift(int dtype, bool exact, bool symmetric, int sched, int R,
                  LiftParams params, LiftJob const *jobs, int njobs,
                  long long total_tiles, cudaStream_t stream);
+// 2 * wavelet + forward when the filters are one of the wavelet tables.
+int wavelet_schedule(std::vector<Filter> const &filters);
+// Shifts 0 .. L-1 (forward) or L-1 .. 0: the level range of hierarchize_in.
+bool canonical_shifts(LiftJob const &job, bool forward);
 
 void cuda_check(cudaError_t e, char const *what);
 size_t dtype_size(int dtype);

@@ -33,6 +33,7 @@ template <typename T, bool ExactProducts> struct Plain {
   static __device__ __forceinline__ Store store(V x) { return x; }
 
   static constexpr bool kHasFp64Mode = false;
+  static constexpr bool kPacked = false;
 
   // C1: the middle coefficient is exactly 1 (skips one multiply).
   // F64: unused (plain arithmetic has a single precision).
@@ -132,6 +133,8 @@ template <bool Sym> struct CompensatedT {
     return __fadd_rn(x.h, x.l);
   }
   static constexpr bool kHasFp64Mode = true;
+  // Wavelet schedules may run the fine levels on packed pairs (sym_update2).
+  static constexpr bool kPacked = Sym;
 
   static __device__ __forceinline__ double to_double(DF x) {
     return double(x.h) + double(x.l);
@@ -168,5 +171,78 @@ template <bool Sym> struct CompensatedT {
 };
 using Compensated = CompensatedT<false>;
 using CompensatedSym = CompensatedT<true>;
+
+// ---------------------------------------------------------------------------
+// Packed pairs of floats for the f32x2 instructions of sm_100+ (one issue
+// slot computes two lanes' values). A pair lives in one 64-bit register.
+using f2 = unsigned long long;
+
+__device__ __forceinline__ f2 f2_pack(float x, float y) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+  return r;
+}
+__device__ __forceinline__ float f2_x(f2 r) {
+  float x, y;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(r));
+  return x;
+}
+__device__ __forceinline__ float f2_y(f2 r) {
+  float x, y;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(r));
+  return y;
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+  f2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// Two double-float values (h.x + l.x, h.y + l.y).
+struct DF2 {
+  f2 h, l;
+};
+
+__device__ __forceinline__ DF2 two_sum2(f2 a, f2 b) {
+  f2 const s = f2_add(a, b);
+  f2 const bb = f2_sub(s, a);
+  f2 const e = f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb));
+  return {s, e};
+}
+
+// The symmetric exact-scaler update of CompensatedT<true> on two values at
+// once (same operations, same roundings per lane).
+template <bool C1>
+__device__ __forceinline__ DF2 sym_update2(Coeffs const &c, DF2 lo, DF2 me,
+                                           DF2 up) {
+  f2 const cc = f2_pack(c.f0, c.f0);
+  DF2 const s = two_sum2(lo.h, up.h);
+  f2 const e1 = f2_add(s.l, f2_add(lo.l, up.l));
+  f2 const t = f2_mul(cc, s.h);
+  f2 m = me.h;
+  if constexpr (!C1) m = f2_mul(f2_pack(c.f1, c.f1), me.h);
+  DF2 const r = two_sum2(m, t);
+  f2 l = f2_fma(cc, e1, r.l);
+  if constexpr (C1)
+    l = f2_add(l, me.l);
+  else
+    l = f2_fma(f2_pack(c.f1, c.f1), me.l, l);
+  return {r.h, l};
+}
 
 } // namespace pgb

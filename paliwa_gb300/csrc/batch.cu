@@ -142,7 +142,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
           L.points += st->job.columns << st->job.log2_n;
           all_jobs.push_back(job);
         }
-        if (L.R >= 2 && L.tiles > 0) dr.launches.push_back(L);
+        if (L.R != 0 && L.tiles > 0) dr.launches.push_back(L);
       }
     }
   }

@@ -150,7 +150,8 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts,
     size_t const count =
         std::min(shifts.size() - first, static_cast<size_t>(kMaxLevels));
     Stage st;
-    st.R = R;
+    // Pencils that one thread holds whole run on the direct kernel.
+    st.R = (R == (1 << v.log2_n)) ? -R : R;
     st.job = make_job(v, shifts, first, count);
     st.job.periodic = 1;
     st.job.log2_window = v.log2_n;
@@ -286,7 +287,7 @@ bool canonical_shifts(LiftJob const &job, bool forward) {
 void launch_lift(int dtype, bool exact, bool symmetric, int sched, int R,
                  LiftParams params, LiftJob const *jobs, int njobs,
                  long long total_tiles, cudaStream_t s) {
-  if (total_tiles <= 0 || R < 2) return;
+  if (total_tiles <= 0 || R == 0) return;
   params.jobs = jobs;
   params.njobs = njobs;
   params.total_tiles = total_tiles;

@@ -13,17 +13,19 @@ namespace pgb {
 
 int device_sms();
 
-template <class A, int R, class Sched>
+template <class A, int R, class Sched, bool Direct>
 void launch_r(LiftParams const &p, cudaStream_t s) {
-  auto kernel = lift_kernel<A, R, kThreads, Sched>;
-  size_t const smem = lift_smem_bytes<A, R, kThreads>(kRounds);
+  auto kernel = lift_kernel<A, R, kThreads, Sched, Direct>;
+  // Direct kernels keep pencils in registers and need no staging memory.
+  size_t const smem = Direct ? 0 : lift_smem_bytes<A, R, kThreads>(kRounds);
   static thread_local int per_sm = 0;
   static thread_local int sms = 0;
   if (per_sm == 0) {
-    cuda_check(cudaFuncSetAttribute(kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)),
-               "cudaFuncSetAttribute");
+    if (smem > 0)
+      cuda_check(cudaFuncSetAttribute(
+                     kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                     static_cast<int>(smem)),
+                 "cudaFuncSetAttribute");
     cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                    &per_sm, kernel, kThreads, smem),
                "occupancy query");
@@ -36,13 +38,16 @@ void launch_r(LiftParams const &p, cudaStream_t s) {
   cuda_check(cudaGetLastError(), "lift_kernel launch");
 }
 
+// R > 0: staged tiles with chunks of R points; R < 0: direct pencils of
+// -R points (one per thread).
 template <class A, class Sched>
 void launch_sched(int R, LiftParams const &p, cudaStream_t s) {
   switch (R) {
-  case 2: return launch_r<A, 2, Sched>(p, s);
-  case 4: return launch_r<A, 4, Sched>(p, s);
-  case 8: return launch_r<A, 8, Sched>(p, s);
-  case 16: return launch_r<A, 16, Sched>(p, s);
+  case -2: return launch_r<A, 2, Sched, true>(p, s);
+  case -4: return launch_r<A, 4, Sched, true>(p, s);
+  case -8: return launch_r<A, 8, Sched, true>(p, s);
+  case -16: return launch_r<A, 16, Sched, true>(p, s);
+  case 16: return launch_r<A, 16, Sched, false>(p, s);
   }
   throw StatusError(2, "bad chunk size");
 }

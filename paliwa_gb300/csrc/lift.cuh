@@ -383,6 +383,103 @@ template <int W, bool FWD> struct WaveletSched {
     }
   }
 
+  // ---- packed variant (A::kPacked): registers hold pairs (slot x,
+  // slot x + R/2) so that fine steps of distance <= R/4 update two points
+  // per f32x2 instruction.
+  template <class A, int R, int NT, int K, class P>
+  static __device__ __forceinline__ void fine_pass_packed(DF2 (&q)[R / 2],
+                                                          RoundCtx<A, NT> &ctx) {
+    using V = typename A::V;
+    constexpr int H = R / 2;
+    constexpr int S = 1 << K;
+    constexpr Coeffs cf = P::coeffs();
+    if constexpr (2 * S <= H) {
+      if constexpr (P::offset == 1) {
+        V const pub = {f2_x(q[0].h), f2_x(q[0].l)};  // slot 0
+        V const nb = ctx.fine_neighbor(1, pub);       // next chunk's slot 0
+#pragma unroll
+        for (int x = S; x < H; x += 2 * S) {
+          DF2 up;
+          if (x + S < H)
+            up = q[(x + S) % H];
+          else  // slots (H, R): this chunk's slot H, next chunk's slot 0
+            up = {f2_pack(f2_y(q[0].h), nb.h), f2_pack(f2_y(q[0].l), nb.l)};
+          q[x] = sym_update2<P::c1one>(cf, q[x - S], q[x], up);
+        }
+      } else {
+        V const pub = {f2_y(q[H - S].h), f2_y(q[H - S].l)};  // slot R - S
+        V const nb = ctx.fine_neighbor(0, pub);  // previous chunk's R - S
+#pragma unroll
+        for (int x = 0; x < H; x += 2 * S) {
+          DF2 lo;
+          if (x >= S)
+            lo = q[(x + H - S) % H];
+          else  // slots (-S, H - S)
+            lo = {f2_pack(nb.h, f2_x(q[H - S].h)),
+                  f2_pack(nb.l, f2_x(q[H - S].l))};
+          q[x] = sym_update2<P::c1one>(cf, lo, q[x], q[x + S]);
+        }
+        ctx.fine_wrote_heads(0);
+      }
+    } else {  // S == H: the two halves' first slots, one scalar update
+      V s0 = {f2_x(q[0].h), f2_x(q[0].l)};  // slot 0
+      V sH = {f2_y(q[0].h), f2_y(q[0].l)};  // slot H
+      if constexpr (P::offset == 1) {
+        V const nb = ctx.fine_neighbor(1, s0);
+        sH = A::template update<P::c1one, false>(cf, s0, sH, nb);
+      } else {
+        V const nb = ctx.fine_neighbor(0, sH);  // previous chunk's slot H
+        s0 = A::template update<P::c1one, false>(cf, nb, s0, sH);
+        ctx.fine_wrote_heads(0);
+      }
+      q[0].h = f2_pack(s0.h, sH.h);
+      q[0].l = f2_pack(s0.l, sH.l);
+    }
+  }
+
+  template <class A, int R, int NT, int K, class... P>
+  static __device__ __forceinline__ void fine_level_packed(
+      DF2 (&q)[R / 2], RoundCtx<A, NT> &ctx, PassList<P...>) {
+    (fine_pass_packed<A, R, NT, K, P>(q, ctx), ...);
+  }
+  template <class A, int R, int NT, int K>
+  static __device__ __forceinline__ void fine_up_packed(DF2 (&q)[R / 2],
+                                                        RoundCtx<A, NT> &ctx,
+                                                        int L) {
+    if constexpr ((1 << K) < R) {
+      if (K < L) {
+        fine_level_packed<A, R, NT, K>(q, ctx, Passes{});
+        fine_up_packed<A, R, NT, K + 1>(q, ctx, L);
+      }
+    }
+  }
+  template <class A, int R, int NT, int K>
+  static __device__ __forceinline__ void fine_down_packed(
+      DF2 (&q)[R / 2], RoundCtx<A, NT> &ctx, int L) {
+    if constexpr (K >= 0) {
+      if (K < L) fine_level_packed<A, R, NT, K>(q, ctx, Passes{});
+      fine_down_packed<A, R, NT, K - 1>(q, ctx, L);
+    }
+  }
+  // Coarse levels act on slot 0 only: unpack it, run them, pack it back.
+  template <class A, int R, int NT>
+  static __device__ __forceinline__ void coarse_packed(DF2 (&q)[R / 2],
+                                                       RoundCtx<A, NT> &ctx,
+                                                       int sh_first,
+                                                       int sh_last, int step) {
+    using V = typename A::V;
+    constexpr int LOG2R = Log2<R>::value;
+    if ((step > 0 && sh_first > sh_last) || (step < 0 && sh_first < sh_last))
+      return;
+    V s0[1] = {{f2_x(q[0].h), f2_x(q[0].l)}};
+    for (int sh = sh_first;; sh += step) {
+      coarse_level<A, 1, NT>(s0, ctx, 1 << (sh - LOG2R), Passes{});
+      if (sh == sh_last) break;
+    }
+    q[0].h = f2_pack(s0[0].h, f2_y(q[0].h));
+    q[0].l = f2_pack(s0[0].l, f2_y(q[0].l));
+  }
+
   template <class A, int R, int NT>
   static __device__ __forceinline__ void run(typename A::V (&v)[R],
                                              RoundCtx<A, NT> &ctx,
@@ -390,6 +487,28 @@ template <int W, bool FWD> struct WaveletSched {
                                              LiftParams const &) {
     constexpr int LOG2R = Log2<R>::value;
     int const L = job.nlevels;
+    if constexpr (A::kPacked && R >= 4) {
+      constexpr int H = R / 2;
+      DF2 q[H];
+#pragma unroll
+      for (int x = 0; x < H; ++x) {
+        q[x].h = f2_pack(v[x].h, v[x + H].h);
+        q[x].l = f2_pack(v[x].l, v[x + H].l);
+      }
+      if constexpr (FWD) {
+        fine_up_packed<A, R, NT, 0>(q, ctx, L);
+        coarse_packed<A, R, NT>(q, ctx, LOG2R, L - 1, 1);
+      } else {
+        coarse_packed<A, R, NT>(q, ctx, L - 1, LOG2R, -1);
+        fine_down_packed<A, R, NT, LOG2R - 1>(q, ctx, L);
+      }
+#pragma unroll
+      for (int x = 0; x < H; ++x) {
+        v[x] = {f2_x(q[x].h), f2_x(q[x].l)};
+        v[x + H] = {f2_y(q[x].h), f2_y(q[x].l)};
+      }
+      return;
+    }
     if constexpr (FWD) {
       fine_up<A, R, NT, 0>(v, ctx, L);
       for (int sh = LOG2R; sh < L; ++sh)
@@ -401,6 +520,51 @@ template <int W, bool FWD> struct WaveletSched {
     }
   }
 };
+
+// R values of one pencil: 16-byte vectors when contiguous and aligned,
+// otherwise element by element at stride kstride.
+template <typename S, int R>
+__device__ __forceinline__ void load_chunk(S const *p, long long kstride,
+                                           bool vec, S (&out)[R]) {
+  constexpr int PER = 16 / sizeof(S);
+  if constexpr (R % PER == 0) {
+    if (vec) {
+#pragma unroll
+      for (int q = 0; q < R / PER; ++q) {
+        uint4 u = *reinterpret_cast<uint4 const *>(p + q * PER);
+        S tmp[PER];
+        memcpy(tmp, &u, 16);
+#pragma unroll
+        for (int e = 0; e < PER; ++e) out[q * PER + e] = tmp[e];
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < R; ++j) out[j] = p[j * kstride];
+}
+
+template <typename S, int R>
+__device__ __forceinline__ void store_chunk(S *p, long long kstride, bool vec,
+                                            S const (&in)[R]) {
+  constexpr int PER = 16 / sizeof(S);
+  if constexpr (R % PER == 0) {
+    if (vec) {
+#pragma unroll
+      for (int q = 0; q < R / PER; ++q) {
+        S tmp[PER];
+#pragma unroll
+        for (int e = 0; e < PER; ++e) tmp[e] = in[q * PER + e];
+        uint4 u;
+        memcpy(&u, tmp, 16);
+        *reinterpret_cast<uint4 *>(p + q * PER) = u;
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < R; ++j) p[j * kstride] = in[j];
+}
 
 // Copies one tile between global memory and the staging layout.
 //
@@ -545,7 +709,11 @@ template <typename S, int R, int NT> struct TileCopy {
   }
 };
 
-template <class A, int R, int NT, class Sched>
+// Direct: every job of the launch is a periodic pencil of n == R points held
+// by one thread (no staging); otherwise tiles are staged through shared
+// memory. The two paths are separate instantiations so that neither's
+// register budget constrains the other.
+template <class A, int R, int NT, class Sched, bool Direct>
 __global__ void __launch_bounds__(NT)
     lift_kernel(__grid_constant__ const LiftParams p) {
   using V = typename A::V;
@@ -602,6 +770,40 @@ __global__ void __launch_bounds__(NT)
 
     unsigned char *const gbase = reinterpret_cast<unsigned char *>(job->base);
 
+    if constexpr (Direct) {
+      // Whole pencil per thread (n == R): straight between HBM and registers,
+      // lanes along columns, no staging and no barrier.
+      bool const vec = job->log2_kstride == 0 &&
+                       ((job->base | job->dst_base) & 15ull) == 0;
+      long long const kstride = 1LL << job->log2_kstride;
+      int const log2B = job->log2_inner;
+      for (int r = 0; r < rounds; ++r) {
+        long long const gc = gc0 + r * NT + t;
+        if (gc >= job->columns) continue;
+        long long const off = ((gc >> log2B) << job->log2_astride) +
+                              (gc & ((1LL << log2B) - 1));
+        V v[R];
+        {
+          S raw[R];
+          load_chunk<S, R>(reinterpret_cast<S const *>(gbase) + off, kstride,
+                           vec, raw);
+#pragma unroll
+          for (int j = 0; j < R; ++j) v[j] = A::load(raw[j]);
+        }
+        RoundCtx<A, NT> ctx(t, 0, 1, 0, lane, periodic, heads, xch);
+        Sched::template run<A, R, NT>(v, ctx, *job, p);
+        {
+          S raw[R];
+#pragma unroll
+          for (int j = 0; j < R; ++j) raw[j] = A::store(v[j]);
+          store_chunk<S, R>(reinterpret_cast<S *>(job->dst_base) + off,
+                            kstride, vec, raw);
+        }
+      }
+      continue;
+    } else {
+    (void)G;
+
     // ---- load: global -> stage
     TileCopy<S, R, NT> cp(*job, periodic, log2W, cols, gc0, wstart, n, pitch,
                           gbase);
@@ -626,6 +828,7 @@ __global__ void __launch_bounds__(NT)
 
     // ---- store: stage -> global (only this tile's segment of a window)
     cp.template run<true>(stage, t, seg, job->halo, job->seg_len);
+    }
   }
 }
 

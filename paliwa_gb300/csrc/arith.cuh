@@ -183,13 +183,13 @@ __device__ __forceinline__ f2 f2_pack(float x, float y) {
   return r;
 }
 __device__ __forceinline__ float f2_x(f2 r) {
-  float x, y;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(r));
+  float x;
+  asm("{\n\t.reg .f32 t;\n\tmov.b64 {%0, t}, %1;\n\t}" : "=f"(x) : "l"(r));
   return x;
 }
 __device__ __forceinline__ float f2_y(f2 r) {
-  float x, y;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(r));
+  float y;
+  asm("{\n\t.reg .f32 t;\n\tmov.b64 {t, %0}, %1;\n\t}" : "=f"(y) : "l"(r));
   return y;
 }
 __device__ __forceinline__ f2 f2_add(f2 a, f2 b) {

@@ -25,6 +25,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "arith.cuh"
@@ -611,6 +612,53 @@ template <typename S, int R, int NT> struct TileCopy {
            seg * seg_len + (k - halo) < n;
   }
 
+  // Rows of RL = min(inner, cols) contiguous elements; row rho = (a_off, k);
+  // VW elements per memory access (VW * sizeof(S) <= 16 bytes).
+  template <bool Store, int VW>
+  __device__ __forceinline__ void rows(S *stage, int t, long long seg,
+                                       int halo, int seg_len, int log2RL) const {
+    using U = typename std::conditional<
+        VW * sizeof(S) == 16, uint4,
+        typename std::conditional<VW * sizeof(S) == 8, uint2,
+                                  unsigned>::type>::type;
+    static_assert(VW * sizeof(S) == sizeof(U), "vector width");
+    S *const g = reinterpret_cast<S *>(
+        Store ? reinterpret_cast<unsigned char *>(job.dst_base) : gbase);
+    int const log2B = job.log2_inner;
+    int const log2vpr = log2RL - Log2<VW>::value;
+    int const nvec = (cols << log2W) / VW;
+    long long const a0 = gc0 >> log2B;
+    long long const b0 = gc0 & ((1LL << log2B) - 1);
+    long long const columns = job.columns;
+#pragma unroll 4
+    for (int v = t; v < nvec; v += NT) {
+      int const rho = v >> log2vpr;
+      int const q = v & ((1 << log2vpr) - 1);
+      int const k = rho & ((1 << log2W) - 1);
+      int const a_off = rho >> log2W;
+      int const w0 = (a_off << log2RL) + q * VW;
+      if (gc0 + w0 >= columns) continue;  // whole vector out of range
+      if (Store && !keep(seg, k, halo, seg_len)) continue;
+      long long const off = ((a0 + a_off) << job.log2_astride) + b0 +
+                            (pos(k) << job.log2_kstride) + q * VW;
+      int const sb = sidx(w0, k);
+      if constexpr (Store) {
+        S tmp[VW];
+#pragma unroll
+        for (int i = 0; i < VW; ++i) tmp[i] = stage[sb + i * pitch];
+        U u;
+        memcpy(&u, tmp, sizeof(U));
+        *reinterpret_cast<U *>(g + off) = u;
+      } else {
+        U const u = *reinterpret_cast<U const *>(g + off);
+        S tmp[VW];
+        memcpy(tmp, &u, sizeof(U));
+#pragma unroll
+        for (int i = 0; i < VW; ++i) stage[sb + i * pitch] = tmp[i];
+      }
+    }
+  }
+
   template <bool Store>
   __device__ __forceinline__ void run(S *stage, int t, long long seg,
                                       int halo, int seg_len) const {
@@ -620,42 +668,6 @@ template <typename S, int R, int NT> struct TileCopy {
         Store ? reinterpret_cast<unsigned char *>(job.dst_base) : gbase);
     long long const columns = job.columns;
     bool const aligned = ((job.base | job.dst_base) & 15ull) == 0;
-    int const log2RL = log2B < log2cols ? log2B : log2cols;
-    if (aligned && VEC > 1 && (1 << log2RL) >= VEC) {
-      // rows of RL contiguous elements; row rho = (a_off, k)
-      int const log2vpr = log2RL - Log2<VEC>::value;
-      int const nvec = (cols << log2W) / VEC;
-      long long const a0 = gc0 >> log2B;
-      long long const b0 = gc0 & ((1LL << log2B) - 1);
-#pragma unroll 4
-      for (int v = t; v < nvec; v += NT) {
-        int const rho = v >> log2vpr;
-        int const q = v & ((1 << log2vpr) - 1);
-        int const k = rho & ((1 << log2W) - 1);
-        int const a_off = rho >> log2W;
-        int const w0 = (a_off << log2RL) + q * VEC;
-        if (gc0 + w0 >= columns) continue;  // whole vector out of range
-        if (Store && !keep(seg, k, halo, seg_len)) continue;
-        long long const off = ((a0 + a_off) << job.log2_astride) + b0 +
-                              (pos(k) << job.log2_kstride) + q * VEC;
-        int const sb = sidx(w0, k);
-        if constexpr (Store) {
-          S tmp[VEC];
-#pragma unroll
-          for (int i = 0; i < VEC; ++i) tmp[i] = stage[sb + i * pitch];
-          uint4 u;
-          memcpy(&u, tmp, 16);
-          *reinterpret_cast<uint4 *>(g + off) = u;
-        } else {
-          uint4 const u = *reinterpret_cast<uint4 const *>(g + off);
-          S tmp[VEC];
-          memcpy(tmp, &u, 16);
-#pragma unroll
-          for (int i = 0; i < VEC; ++i) stage[sb + i * pitch] = tmp[i];
-        }
-      }
-      return;
-    }
     if (aligned && VEC > 1 && log2B == 0 && job.log2_kstride == 0 &&
         R >= VEC) {
       // each column contiguous along k
@@ -686,26 +698,18 @@ template <typename S, int R, int NT> struct TileCopy {
       }
       return;
     }
-    // scalar: elements ordered (a, k, b) with b fastest
-    int const log2Bb = log2B < log2cols ? log2B : log2cols;
-    int const total = cols << log2W;
-#pragma unroll 4
-    for (int e = t; e < total; e += NT) {
-      int const bo = e & ((1 << log2Bb) - 1);
-      int const k = (e >> log2Bb) & ((1 << log2W) - 1);
-      int const ao = e >> (log2Bb + log2W);
-      int const w = (ao << log2Bb) | bo;
-      long long const gc = gc0 + w;
-      if (gc >= columns) continue;
-      if (Store && !keep(seg, k, halo, seg_len)) continue;
-      long long const off = ((gc >> log2B) << job.log2_astride) +
-                            (gc & ((1LL << log2B) - 1)) +
-                            (pos(k) << job.log2_kstride);
-      if constexpr (Store)
-        g[off] = stage[sidx(w, k)];
-      else
-        stage[sidx(w, k)] = g[off];
+    int const log2RL = log2B < log2cols ? log2B : log2cols;
+    // Vector width: as wide as the rows and the alignment allow.
+    if constexpr (VEC >= 4) {
+      if (aligned && log2RL >= 2)
+        return rows<Store, 4>(stage, t, seg, halo, seg_len, log2RL);
     }
+    if constexpr (VEC >= 2) {
+      if ((((job.base | job.dst_base) & (2 * sizeof(S) - 1)) == 0) &&
+          log2RL >= 1)
+        return rows<Store, 2>(stage, t, seg, halo, seg_len, log2RL);
+    }
+    rows<Store, 1>(stage, t, seg, halo, seg_len, log2RL);
   }
 };
 

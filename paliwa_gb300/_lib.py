@@ -45,6 +45,8 @@ SIGNATURES = {
         _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _i, _vp]),
     "paliwa_gb_hierarchize": (_i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _vp]),
     "paliwa_gb_dehierarchize": (_i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _vp]),
+    "paliwa_gb_transform_noalloc": (
+        _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _i, _vp]),
     "paliwa_gb_batch_create": (
         _i, [_i, _i, _pi64, _pi64, _pi64, _i, _i, ctypes.POINTER(_vp),
              ctypes.POINTER(_vp)]),

@@ -150,8 +150,12 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts,
     size_t const count =
         std::min(shifts.size() - first, static_cast<size_t>(kMaxLevels));
     Stage st;
-    // Pencils that one thread holds whole run on the direct kernel.
-    st.R = (R == (1 << v.log2_n)) ? -R : R;
+    // Pencils that one thread holds whole, and contiguous pencils (last
+    // axis) that fit one warp, run on the direct kernel.
+    bool const direct = R == (1 << v.log2_n) ||
+                        (v.log2_inner == 0 && v.log2_kstride == 0 &&
+                         log2G <= 5);
+    st.R = direct ? -R : R;
     st.job = make_job(v, shifts, first, count);
     st.job.periodic = 1;
     st.job.log2_window = v.log2_n;

@@ -73,6 +73,9 @@ struct LiftParams {
   LiftJob job;
 };
 
+// Column rounds per staged tile: a tile holds kTileRounds * NT * R points.
+constexpr int kTileRounds = 2;
+
 template <int X> struct Log2 {
   static constexpr int value = 1 + Log2<X / 2>::value;
 };
@@ -522,6 +525,19 @@ template <int W, bool FWD> struct WaveletSched {
   }
 };
 
+// Asynchronous 4- or 8-byte copy from global to shared memory (sm_80+):
+// loads stay in flight without occupying registers.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, void const *gmem) {
+  unsigned const dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst),
+               "l"(gmem), "n"(BYTES)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // R values of one pencil: 16-byte vectors when contiguous and aligned,
 // otherwise element by element at stride kstride.
 template <typename S, int R>
@@ -613,7 +629,9 @@ template <typename S, int R, int NT> struct TileCopy {
   }
 
   // Rows of RL = min(inner, cols) contiguous elements; row rho = (a_off, k);
-  // VW elements per memory access (VW * sizeof(S) <= 16 bytes).
+  // VW elements per memory access (VW * sizeof(S) <= 16 bytes). A tile holds
+  // exactly NT * PER vectors, and every thread issues all of its loads before
+  // it writes any of them to shared memory, to keep PER loads in flight.
   template <bool Store, int VW>
   __device__ __forceinline__ void rows(S *stage, int t, long long seg,
                                        int halo, int seg_len, int log2RL) const {
@@ -622,39 +640,44 @@ template <typename S, int R, int NT> struct TileCopy {
         typename std::conditional<VW * sizeof(S) == 8, uint2,
                                   unsigned>::type>::type;
     static_assert(VW * sizeof(S) == sizeof(U), "vector width");
+    constexpr int PER = kTileRounds * R / VW;  // vectors per thread
     S *const g = reinterpret_cast<S *>(
         Store ? reinterpret_cast<unsigned char *>(job.dst_base) : gbase);
     int const log2B = job.log2_inner;
     int const log2vpr = log2RL - Log2<VW>::value;
-    int const nvec = (cols << log2W) / VW;
     long long const a0 = gc0 >> log2B;
     long long const b0 = gc0 & ((1LL << log2B) - 1);
     long long const columns = job.columns;
-#pragma unroll 4
-    for (int v = t; v < nvec; v += NT) {
+    auto locate = [&](int v, long long &off, int &sb) -> bool {
       int const rho = v >> log2vpr;
       int const q = v & ((1 << log2vpr) - 1);
       int const k = rho & ((1 << log2W) - 1);
       int const a_off = rho >> log2W;
       int const w0 = (a_off << log2RL) + q * VW;
-      if (gc0 + w0 >= columns) continue;  // whole vector out of range
-      if (Store && !keep(seg, k, halo, seg_len)) continue;
-      long long const off = ((a0 + a_off) << job.log2_astride) + b0 +
-                            (pos(k) << job.log2_kstride) + q * VW;
-      int const sb = sidx(w0, k);
+      off = ((a0 + a_off) << job.log2_astride) + b0 +
+            (pos(k) << job.log2_kstride) + q * VW;
+      sb = sidx(w0, k);
+      return gc0 + w0 < columns && (!Store || keep(seg, k, halo, seg_len));
+    };
+#pragma unroll 4
+    for (int i = 0; i < PER; ++i) {
+      long long off;
+      int sb;
+      bool const ok = locate(t + i * NT, off, sb);
+      if (!ok) continue;
       if constexpr (Store) {
         S tmp[VW];
 #pragma unroll
-        for (int i = 0; i < VW; ++i) tmp[i] = stage[sb + i * pitch];
+        for (int e = 0; e < VW; ++e) tmp[e] = stage[sb + e * pitch];
         U u;
         memcpy(&u, tmp, sizeof(U));
         *reinterpret_cast<U *>(g + off) = u;
       } else {
-        U const u = *reinterpret_cast<U const *>(g + off);
-        S tmp[VW];
-        memcpy(tmp, &u, sizeof(U));
+        // element-wise asynchronous copies into the padded layout (the
+        // elements of one vector land `pitch` apart)
 #pragma unroll
-        for (int i = 0; i < VW; ++i) stage[sb + i * pitch] = tmp[i];
+        for (int e = 0; e < VW; ++e)
+          cp_async<sizeof(S)>(stage + sb + e * pitch, g + off + e);
       }
     }
   }
@@ -671,10 +694,11 @@ template <typename S, int R, int NT> struct TileCopy {
     if (aligned && VEC > 1 && log2B == 0 && job.log2_kstride == 0 &&
         R >= VEC) {
       // each column contiguous along k
+      constexpr int PER = kTileRounds * R / VEC;
       int const log2vpc = log2W - Log2<VEC>::value;
-      int const nvec = (cols << log2W) / VEC;
 #pragma unroll 4
-      for (int v = t; v < nvec; v += NT) {
+      for (int i = 0; i < PER; ++i) {
+        int const v = t + i * NT;
         int const w = v >> log2vpc;
         int const k = (v & ((1 << log2vpc) - 1)) * VEC;
         if (gc0 + w >= columns) continue;
@@ -684,16 +708,14 @@ template <typename S, int R, int NT> struct TileCopy {
         if constexpr (Store) {
           S tmp[VEC];
 #pragma unroll
-          for (int i = 0; i < VEC; ++i) tmp[i] = stage[sb + i];
+          for (int e = 0; e < VEC; ++e) tmp[e] = stage[sb + e];
           uint4 u;
           memcpy(&u, tmp, 16);
           *reinterpret_cast<uint4 *>(g + off) = u;
         } else {
-          uint4 const u = *reinterpret_cast<uint4 const *>(g + off);
-          S tmp[VEC];
-          memcpy(tmp, &u, 16);
 #pragma unroll
-          for (int i = 0; i < VEC; ++i) stage[sb + i] = tmp[i];
+          for (int e = 0; e < VEC; ++e)
+            cp_async<sizeof(S)>(stage + sb + e, g + off + e);
         }
       }
       return;
@@ -760,7 +782,7 @@ __global__ void __launch_bounds__(NT)
     int const log2G = log2W - LOG2R;          // chunks per column
     int const G = 1 << log2G;
     int const log2CR = LOG2NT - log2G;        // columns per round
-    int const rounds = p.rounds;
+    constexpr int rounds = kTileRounds;
     int const cols = rounds << log2CR;        // columns per tile
     int const pitch = stage_pitch<R>(G);
     int const periodic = job->periodic;
@@ -775,17 +797,27 @@ __global__ void __launch_bounds__(NT)
     unsigned char *const gbase = reinterpret_cast<unsigned char *>(job->base);
 
     if constexpr (Direct) {
-      // Whole pencil per thread (n == R): straight between HBM and registers,
-      // lanes along columns, no staging and no barrier.
+      // Pencils straight between HBM and registers, no staging and no
+      // barrier: either one whole pencil per thread (n == R, lanes along
+      // columns), or a contiguous pencil (last axis) of G <= 32 chunks held
+      // by G consecutive lanes that exchange by shuffle.
       bool const vec = job->log2_kstride == 0 &&
                        ((job->base | job->dst_base) & 15ull) == 0;
       long long const kstride = 1LL << job->log2_kstride;
       int const log2B = job->log2_inner;
+      int const c = t & (G - 1);
       for (int r = 0; r < rounds; ++r) {
-        long long const gc = gc0 + r * NT + t;
-        if (gc >= job->columns) continue;
+        long long gc = gc0 + (r << log2CR) + (t >> log2G);
+        // A warp skips only as a whole (its lanes shuffle with each other);
+        // lanes past the last column of a partly filled warp recompute the
+        // last column and do not store it.
+        if (gc0 + (r << log2CR) + ((t & ~31) >> log2G) >= job->columns)
+          continue;
+        bool const keep = gc < job->columns;
+        if (!keep) gc = job->columns - 1;
         long long const off = ((gc >> log2B) << job->log2_astride) +
-                              (gc & ((1LL << log2B) - 1));
+                              (gc & ((1LL << log2B) - 1)) +
+                              static_cast<long long>(c) * R * kstride;
         V v[R];
         {
           S raw[R];
@@ -794,14 +826,15 @@ __global__ void __launch_bounds__(NT)
 #pragma unroll
           for (int j = 0; j < R; ++j) v[j] = A::load(raw[j]);
         }
-        RoundCtx<A, NT> ctx(t, 0, 1, 0, lane, periodic, heads, xch);
+        RoundCtx<A, NT> ctx(t, c, G, log2G, lane, periodic, heads, xch);
         Sched::template run<A, R, NT>(v, ctx, *job, p);
         {
           S raw[R];
 #pragma unroll
           for (int j = 0; j < R; ++j) raw[j] = A::store(v[j]);
-          store_chunk<S, R>(reinterpret_cast<S *>(job->dst_base) + off,
-                            kstride, vec, raw);
+          if (keep)
+            store_chunk<S, R>(reinterpret_cast<S *>(job->dst_base) + off,
+                              kstride, vec, raw);
         }
       }
       continue;
@@ -812,6 +845,7 @@ __global__ void __launch_bounds__(NT)
     TileCopy<S, R, NT> cp(*job, periodic, log2W, cols, gc0, wstart, n, pitch,
                           gbase);
     cp.template run<false>(stage, t, seg, 0, 0);
+    cp_async_wait_all();
     __syncthreads();
 
     // ---- compute: one round = NT / G columns, thread = (column, chunk)

@@ -62,7 +62,7 @@ struct Stage {
 
 constexpr int kWindowLog2 = 12;   // points per column per CTA round (4096)
 constexpr int kThreads = 256;
-constexpr int kRounds = 2;        // column rounds per tile
+constexpr int kRounds = kTileRounds;  // column rounds per tile
 constexpr int kHaloBudget = 256;  // halo per side of a window, in points
 
 int chunk_for(int log2_n);        // R for a periodic pencil of 2^log2_n

@@ -360,38 +360,64 @@ def run_gpu(args, w, world, rank, local):
         bt64 = pct.Batch(v64, w.levels, w.lmin, w.lmax, w.wavelet)
         bt32 = pct.Batch(v32, w.levels, w.lmin, w.lmax, w.wavelet,
                          compensated=True)
-        # Accuracy of the compensated FP32 forward transform against FP64.
-        bt64.hierarchize(stream)
-        bt32.hierarchize(stream)
+        # Accuracy of the compensated FP32 forward transform against FP64:
+        # against the FP64 transform of the FP64 inputs (the headline), and
+        # against the FP64 transform of the same FP32-rounded inputs (the
+        # arithmetic and the FP32 storage between axes). The FP64 transform
+        # of the rounded inputs against that of the FP64 inputs is the floor
+        # that rounding the inputs to FP32 alone sets; plain FP32
+        # arithmetic is shown beside it.
+        b64q = b32.double()
+        b32p = b32.clone()
+
+        def views(buf, like):
+            esz = like[0].element_size()
+            return [buf.narrow(0, (v.data_ptr() - like[0].data_ptr()) // esz,
+                               v.numel()) for v in like]
+
+        v64q = views(b64q, v64)
+        v32p = views(b32p, v32)
+        bt64q = pct.Batch(v64q, w.levels, w.lmin, w.lmax, w.wavelet)
+        bt32p = pct.Batch(v32p, w.levels, w.lmin, w.lmax, w.wavelet)
+        for bt in (bt64, bt32, bt64q, bt32p):
+            bt.hierarchize(stream)
         stream.synchronize()
-        err = {"norm": "max|e|/max|ref| and rms(e)/rms(ref) over the grids"}
+        bt64q.close()
+        bt32p.close()
         qs = sorted(set(w.q))
-        per_q = {}
-        off = 0
         # grids are packed in q-major order: group contiguous ranges
         bounds = {}
         for i, (q, v) in enumerate(zip(w.q, v64)):
-            start = v.data_ptr() - b64.data_ptr()
-            bounds.setdefault(q, [start // 8, 0])
-            bounds[q][1] = start // 8 + v.numel()
-        tot_max = tot_ref = 0.0
-        tot_sq = tot_rsq = 0.0
-        for q in qs:
-            lo, hi = bounds[q]
-            r = b64[lo:hi]
-            e = b32[lo:hi].double() - r
-            emax, rmax = float(e.abs().max()), float(r.abs().max())
-            esq, rsq = float(e.pow(2).sum()), float(r.pow(2).sum())
-            per_q[str(q)] = {"max_rel": emax / rmax,
-                             "rms_rel": math.sqrt(esq / rsq)}
-            tot_max, tot_ref = max(tot_max, emax), max(tot_ref, rmax)
-            tot_sq, tot_rsq = tot_sq + esq, tot_rsq + rsq
-            del e
-        err["max_rel"] = tot_max / tot_ref
-        err["rms_rel"] = math.sqrt(tot_sq / tot_rsq)
-        if len(qs) > 1:
-            err["per_q"] = per_q
-        del off
+            start = (v.data_ptr() - v64[0].data_ptr()) // 8
+            bounds.setdefault(q, [start, 0])
+            bounds[q][1] = start + v.numel()
+
+        def rel_errors(test, ref, with_q):
+            out, per_q = {}, {}
+            tot_max = tot_ref = tot_sq = tot_rsq = 0.0
+            for q in qs:
+                lo, hi = bounds[q]
+                r = ref[lo:hi]
+                e = test[lo:hi].double() - r
+                emax, rmax = float(e.abs().max()), float(r.abs().max())
+                esq, rsq = float(e.pow(2).sum()), float(r.pow(2).sum())
+                per_q[str(q)] = {"max_rel": emax / rmax,
+                                 "rms_rel": math.sqrt(esq / rsq)}
+                tot_max, tot_ref = max(tot_max, emax), max(tot_ref, rmax)
+                tot_sq, tot_rsq = tot_sq + esq, tot_rsq + rsq
+                del e
+            out["max_rel"] = tot_max / tot_ref
+            out["rms_rel"] = math.sqrt(tot_sq / tot_rsq)
+            if with_q and len(qs) > 1:
+                out["per_q"] = per_q
+            return out
+
+        err = {"norm": "max|e|/max|ref| and rms(e)/rms(ref) over the grids"}
+        err.update(rel_errors(b32, b64, True))
+        err["same_fp32_inputs"] = rel_errors(b32, b64q, False)
+        err["input_rounding_floor"] = rel_errors(b64q, b64, False)
+        err["plain_fp32"] = rel_errors(b32p, b64, False)
+        del b64q, b32p, v64q, v32p
 
         # Combine / restrict in FP64 (sparse grid of the kept subspaces).
         combine = None
@@ -432,8 +458,8 @@ def run_gpu(args, w, world, rank, local):
         for name, bt in (("f32c", bt32), ("f64", bt64)):
             rows = []
             for fwd in (True, False):
-                ms, by = bt.profile(fwd, stream)
-                rows += list(zip(ms, by))
+                ms, by, kd = bt.profile(fwd, stream)
+                rows += list(zip(ms, by, kd))
             prof[name] = rows
         nlaunch = sum(bt32.launches())
 
@@ -443,6 +469,18 @@ def run_gpu(args, w, world, rank, local):
     value = pts_step * args.steps / (ms32 / 1e3)
     value64 = pts_step * args.steps / (ms64 / 1e3)
     peak, peak_kind = peaks()
+
+    def by_kernel(rows, peak):
+        """Time share and HBM fraction of each kernel over one step."""
+        out = {}
+        tot = sum(r[0] for r in rows)
+        for ms, by, code in rows:
+            k = out.setdefault(pct.kernel_name(code), [0.0, 0])
+            k[0] += ms
+            k[1] += by
+        return {name: {"share": ms / tot,
+                       "frac": by / (ms / 1e3) / 1e9 / peak}
+                for name, (ms, by) in sorted(out.items())}
 
     def roof(rows):
         top = max(rows, key=lambda r: r[0])
@@ -502,7 +540,9 @@ def run_gpu(args, w, world, rank, local):
                 "bound": "hbm", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                 "peak_kind": peak_kind,
-                "kernel": "lift_kernel<CompensatedSym> (largest launch)",
+                "kernel": pct.kernel_name(top32[2]) + ", FP32c (largest "
+                          "launch)",
+                "by_kernel": by_kernel(prof["f32c"], peak),
                 "bytes_per_launch": top32[1], "launch_ms": top32[0],
                 "all_launches_frac":
                     tot32_b / (tot32_ms / 1e3) / 1e9 / peak},

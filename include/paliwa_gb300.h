@@ -163,11 +163,15 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
                          int64_t *launches_inverse);
 /* Runs one direction (forward != 0: hierarchize) launch by launch with CUDA
  * events around each launch, waits for it, and reports each launch's
- * duration and algorithmic bytes (one read and one write of every grid point
- * it stores). Call with capacity 0 to get *nlaunches first. */
+ * duration, algorithmic bytes (one read and one write of every grid point
+ * it stores) and kernel: R > 0 the staged kernel with chunks of R points,
+ * -R the direct kernel (pencils in registers), 64 + R and 128 + R the wide
+ * kernel (rows of adjacent columns in registers) on a strided axis and on
+ * the last axis; `kernels` may be null. Call with
+ * capacity 0 to get *nlaunches first. */
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,
-                            int64_t *bytes);
+                            int64_t *bytes, int32_t *kernels);
 void paliwa_gb_batch_destroy(paliwa_gb_batch *batch);
 
 /* ------------------------------------------------------------------------

@@ -56,7 +56,8 @@ SIGNATURES = {
     "paliwa_gb_batch_info": (_i, [_vp, _pi64, _pi64, _pi64]),
     "paliwa_gb_batch_profile": (
         _i, [_vp, _i, _vp, _i, ctypes.POINTER(_i),
-             ctypes.POINTER(ctypes.c_float), _pi64]),
+             ctypes.POINTER(ctypes.c_float), _pi64,
+             ctypes.POINTER(ctypes.c_int32)]),
     "paliwa_gb_batch_destroy": (None, [_vp]),
     "paliwa_gb_ct_create": (
         _i, [_i, _i, _pi64, _pd, _pi64, _i, ctypes.POINTER(_vp), _i,

@@ -213,6 +213,23 @@ __device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
   return d;
 }
 
+// A pair of equal floats, built with integer operations so that the
+// compiler folds it when x is a constant.
+__device__ __forceinline__ f2 f2_splat(float x) {
+  unsigned long long const b = __float_as_uint(x);
+  return b | (b << 32);
+}
+// A pair from two raw 32-bit words (x in the low half) and back.
+__device__ __forceinline__ f2 f2_bits(unsigned x, unsigned y) {
+  return static_cast<f2>(x) | (static_cast<f2>(y) << 32);
+}
+__device__ __forceinline__ unsigned f2_lo(f2 r) {
+  return static_cast<unsigned>(r);
+}
+__device__ __forceinline__ unsigned f2_hi(f2 r) {
+  return static_cast<unsigned>(r >> 32);
+}
+
 // Two double-float values (h.x + l.x, h.y + l.y).
 struct DF2 {
   f2 h, l;
@@ -230,19 +247,102 @@ __device__ __forceinline__ DF2 two_sum2(f2 a, f2 b) {
 template <bool C1>
 __device__ __forceinline__ DF2 sym_update2(Coeffs const &c, DF2 lo, DF2 me,
                                            DF2 up) {
-  f2 const cc = f2_pack(c.f0, c.f0);
+  f2 const cc = f2_splat(c.f0);
   DF2 const s = two_sum2(lo.h, up.h);
   f2 const e1 = f2_add(s.l, f2_add(lo.l, up.l));
   f2 const t = f2_mul(cc, s.h);
   f2 m = me.h;
-  if constexpr (!C1) m = f2_mul(f2_pack(c.f1, c.f1), me.h);
+  if constexpr (!C1) m = f2_mul(f2_splat(c.f1), me.h);
   DF2 const r = two_sum2(m, t);
   f2 l = f2_fma(cc, e1, r.l);
   if constexpr (C1)
     l = f2_add(l, me.l);
   else
-    l = f2_fma(f2_pack(c.f1, c.f1), me.l, l);
+    l = f2_fma(f2_splat(c.f1), me.l, l);
   return {r.h, l};
 }
+
+// ---------------------------------------------------------------------------
+// Rows of adjacent columns, for the wide kernel (lift.cuh). A thread holds
+// kCols adjacent pencils of a strided axis; one value V is the row of kCols
+// points at the same pencil position, loaded and stored as one vector
+// (Store), and every operation acts on each column exactly as the scalar
+// policy named below does, so results are bit-identical to it.
+
+// Plain<float, true> on four columns: two f32x2 pairs (columns 0-1, 2-3).
+struct F32Row4 {
+  f2 a, b;
+};
+struct RowF32 {
+  using V = F32Row4;
+  using Store = uint4;
+  using Elem = float;
+  static constexpr int kCols = 4;
+  static constexpr bool kHasFp64Mode = false;
+  static constexpr bool kPacked = false;
+  static __device__ __forceinline__ V load(Store u) {
+    return {f2_bits(u.x, u.y), f2_bits(u.z, u.w)};
+  }
+  static __device__ __forceinline__ Store store(V v) {
+    return {f2_lo(v.a), f2_hi(v.a), f2_lo(v.b), f2_hi(v.b)};
+  }
+  // fma(c2, up, fma(c0, lo, c1 * me)) per column (Plain<float, true>).
+  template <bool C1>
+  static __device__ __forceinline__ f2 pair(Coeffs const &c, f2 lo, f2 me,
+                                            f2 up) {
+    f2 t = C1 ? me : f2_mul(f2_splat(c.f1), me);
+    t = f2_fma(f2_splat(c.f0), lo, t);
+    return f2_fma(f2_splat(c.f2), up, t);
+  }
+  template <bool C1, bool F64>
+  static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
+                                             V up) {
+    return {pair<C1>(c, lo.a, me.a, up.a), pair<C1>(c, lo.b, me.b, up.b)};
+  }
+};
+
+// CompensatedT<true> on two columns: one DF2 (sym_update2).
+struct RowF32C {
+  using V = DF2;
+  using Store = uint2;
+  using Elem = float;
+  static constexpr int kCols = 2;
+  static constexpr bool kHasFp64Mode = false;
+  static constexpr bool kPacked = false;
+  static __device__ __forceinline__ V load(Store u) {
+    return {f2_bits(u.x, u.y), 0ull};
+  }
+  static __device__ __forceinline__ Store store(V v) {
+    f2 const s = f2_add(v.h, v.l);
+    return {f2_lo(s), f2_hi(s)};
+  }
+  template <bool C1, bool F64>
+  static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
+                                             V up) {
+    return sym_update2<C1>(c, lo, me, up);
+  }
+};
+
+// Plain<double, true> on two columns.
+struct F64Row2 {
+  double x, y;
+};
+struct RowF64 {
+  using V = F64Row2;
+  using Store = double2;
+  using Elem = double;
+  static constexpr int kCols = 2;
+  static constexpr bool kHasFp64Mode = false;
+  static constexpr bool kPacked = false;
+  static __device__ __forceinline__ V load(Store u) { return {u.x, u.y}; }
+  static __device__ __forceinline__ Store store(V v) { return {v.x, v.y}; }
+  template <bool C1, bool F64>
+  static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
+                                             V up) {
+    using P = Plain<double, true>;
+    return {P::template update<C1, F64>(c, lo.x, me.x, up.x),
+            P::template update<C1, F64>(c, lo.y, me.y, up.y)};
+  }
+};
 
 } // namespace pgb

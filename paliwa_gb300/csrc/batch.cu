@@ -106,8 +106,9 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
     size_t shadow_off = 0;
     for (int g = 0; g < b.ngrids; ++g) {
       int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
-      AxisView view = axis_view(
-          reinterpret_cast<unsigned long long>(grid_ptrs[g]), b.ndim, lv, d);
+      AxisView view =
+          axis_view(reinterpret_cast<unsigned long long>(grid_ptrs[g]),
+                    b.ndim, lv, d, b.dtype);
       auto const shifts = level_shifts(lv[d], lmin[d], forward);
       if (needs_shadow(view, shifts)) {
         size_t bytes = es;
@@ -425,7 +426,7 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
 
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,
-                            int64_t *bytes) {
+                            int64_t *bytes, int32_t *kernels) {
   return guarded([&] {
     if (batch == nullptr || nlaunches == nullptr)
       throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
@@ -444,6 +445,7 @@ int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                   dr.params, dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
       cuda_check(cudaEventRecord(ev[i + 1], s), "cudaEventRecord");
       bytes[i] = static_cast<int64_t>(2 * es) * L.points;
+      if (kernels != nullptr) kernels[i] = L.R;
     }
     cuda_check(cudaEventSynchronize(ev[n]), "cudaEventSynchronize");
     for (int i = 0; i < n; ++i)

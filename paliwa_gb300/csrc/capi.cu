@@ -53,6 +53,20 @@ int chunk_for(int log2_n) {
   return 16;
 }
 
+// Points per thread and column of the wide kernel (0: pencil too long for
+// it). Pencils of up to 16 points are held whole by one thread; pencils of
+// 32 and 64 points by G = 4 lanes, so that a warp row is 8 column groups
+// (32 or 64 contiguous bytes). With more lanes per pencil each warp load
+// touches more distinct rows with fewer bytes each (16 lanes: 16-byte
+// pieces; 32 lanes: 8): measured on a 2^26-point FP32 grid, the first axis
+// at n = 256 fell from 2.2 TB/s (G = 16) to 0.47 TB/s (G = 32), so longer
+// pencils go to the staged kernel.
+int wide_chunk(int log2_n) {
+  if (log2_n <= 4) return 1 << log2_n;
+  if (log2_n <= 6) return 1 << (log2_n - 2);
+  return 0;
+}
+
 void cuda_check(cudaError_t e, char const *what) {
   if (e != cudaSuccess)
     throw StatusError(PALIWA_GB_CUDA_ERROR,
@@ -69,8 +83,13 @@ size_t dtype_size(int dtype) {
 }
 
 AxisView axis_view(unsigned long long base, int ndim, int64_t const *level,
-                   int dim) {
+                   int dim, int dtype) {
   AxisView v;
+  // Row vectors of the wide kernel: 4 floats (FP32), 2 floats (FP32
+  // compensated: a row is one double-float pair of pairs), 2 doubles (FP64).
+  int const log2_row = dtype == PALIWA_GB_F32 ? 2 : 1;
+  v.log2_row = (base % 16) == 0 ? log2_row : 0;
+  v.wide_last = dtype == PALIWA_GB_F32C;
   int log2_outer = 0, log2_inner = 0;
   for (int d = 0; d < dim; ++d) log2_outer += static_cast<int>(level[d]);
   for (int d = dim + 1; d < ndim; ++d) log2_inner += static_cast<int>(level[d]);
@@ -140,26 +159,49 @@ LiftJob make_job(AxisView const &v, std::vector<int> const &sh, size_t first,
 }
 
 // Periodic whole-pencil stages; level lists longer than one job holds are
-// split into consecutive stages (order preserved).
-void plan_periodic(AxisView const &v, std::vector<int> const &shifts,
+// split into consecutive stages (order preserved). `ws` is the wavelet
+// schedule of the filters (or -1).
+void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
                    std::vector<Stage> &out) {
   int const R = chunk_for(v.log2_n);
   int const log2G = v.log2_n - (31 - __builtin_clz(R));
   long long const C = static_cast<long long>(kRounds) * (kThreads >> log2G);
+  int const wR = wide_chunk(v.log2_n);
+  int const wlog2G = wR > 0 ? v.log2_n - (31 - __builtin_clz(wR)) : 0;
+  long long const wC = static_cast<long long>(kRounds) * (kThreads >> wlog2G);
   for (size_t first = 0; first < shifts.size(); first += kMaxLevels) {
     size_t const count =
         std::min(shifts.size() - first, static_cast<size_t>(kMaxLevels));
     Stage st;
-    // Pencils that one thread holds whole, and contiguous pencils (last
-    // axis) that fit one warp, run on the direct kernel.
-    bool const direct = R == (1 << v.log2_n) ||
-                        (v.log2_inner == 0 && v.log2_kstride == 0 &&
-                         log2G <= 5);
-    st.R = direct ? -R : R;
     st.job = make_job(v, shifts, first, count);
     st.job.periodic = 1;
     st.job.log2_window = v.log2_n;
-    st.job.col_tiles = ceil_div(v.columns, C);
+    // The wide kernel (wavelet schedules on grids aligned to 16 bytes):
+    // strided pencils of up to 64 points whose rows hold a whole row vector
+    // of adjacent columns, and (FP32 compensated) last-axis pencils of up to
+    // 512 points when there are at least a row vector's worth of them
+    // (measured on 2^26-point grids, FP32c last axis: 3.0-4.5 TB/s against
+    // 2.8-4.1 on the direct kernel). Otherwise pencils
+    // that one thread holds whole, and last-axis pencils that fit one warp,
+    // run on the direct kernel; the rest staged.
+    bool const canon = ws >= 0 && v.log2_row > 0 &&
+                       canonical_shifts(st.job, (ws & 1) != 0);
+    bool const last = v.log2_inner == 0 && v.log2_kstride == 0;
+    bool const wide = canon && wR > 0 && !last &&
+                      v.log2_inner >= v.log2_row;
+    bool const wide_last = canon && last && v.wide_last && log2G <= 5 &&
+                           v.columns >= (1LL << v.log2_row);
+    bool const direct = R == (1 << v.log2_n) || (last && log2G <= 5);
+    if (wide) {
+      st.R = kWide + wR;
+      st.job.col_tiles = ceil_div(v.columns >> v.log2_row, wC);
+    } else if (wide_last) {
+      st.R = kWideContig + R;
+      st.job.col_tiles = ceil_div(v.columns >> v.log2_row, C);
+    } else {
+      st.R = direct ? -R : R;
+      st.job.col_tiles = ceil_div(v.columns, C);
+    }
     st.tiles = st.job.col_tiles;
     out.push_back(st);
   }
@@ -231,7 +273,7 @@ void plan_axis(AxisView const &view, std::vector<int> const &shifts,
                std::vector<Filter> const &filters, std::vector<Stage> &out) {
   if (shifts.empty() || filters.empty() || view.log2_n == 0) return;
   if (view.log2_n <= kWindowLog2) {
-    plan_periodic(view, shifts, out);
+    plan_periodic(view, shifts, wavelet_schedule(filters), out);
     return;
   }
   // Long pencil: levels closer than 2^m run on windows with a halo of at most
@@ -297,6 +339,14 @@ void launch_lift(int dtype, bool exact, bool symmetric, int sched, int R,
   params.total_tiles = total_tiles;
   params.rounds = kRounds;
   if (params.fp64_log2_points >= 0) sched = -1;
+  if (R > kWide) {  // both layouts of the wide kernel
+    switch (dtype) {
+    case PALIWA_GB_F64: return launch_wide_f64(sched, R, params, s);
+    case PALIWA_GB_F32: return launch_wide_f32(sched, R, params, s);
+    case PALIWA_GB_F32C: return launch_wide_f32c(sched, R, params, s);
+    }
+    throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
+  }
   switch (dtype) {
   case PALIWA_GB_F64: return launch_lift_f64(exact, sched, R, params, s);
   case PALIWA_GB_F32: return launch_lift_f32(exact, sched, R, params, s);
@@ -338,8 +388,8 @@ void transform_axis(void *grid, int dtype, int ndim, int64_t const *level,
                     int dim, std::vector<int> const &shifts,
                     std::vector<Filter> const &filters, cudaStream_t s) {
   LiftParams const params = launch_params(filters);
-  AxisView view =
-      axis_view(reinterpret_cast<unsigned long long>(grid), ndim, level, dim);
+  AxisView view = axis_view(reinterpret_cast<unsigned long long>(grid), ndim,
+                            level, dim, dtype);
   void *shadow = nullptr;
   if (needs_shadow(view, shifts)) {
     // Stream-ordered scratch for the windowed stages of long pencils.

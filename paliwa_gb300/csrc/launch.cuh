@@ -13,13 +13,12 @@ namespace pgb {
 
 int device_sms();
 
-template <class A, int R, class Sched, bool Direct>
-void launch_r(LiftParams const &p, cudaStream_t s) {
-  auto kernel = lift_kernel<A, R, kThreads, Sched, Direct>;
-  // Direct kernels keep pencils in registers and need no staging memory.
-  size_t const smem = Direct ? 0 : lift_smem_bytes<A, R, kThreads>(kRounds);
-  static thread_local int per_sm = 0;
-  static thread_local int sms = 0;
+// One persistent launch: as many CTAs as fit on the device at once, or one
+// per tile when there are fewer tiles. `per_sm` and `sms` cache the
+// occupancy of this kernel (one pair per kernel instantiation).
+template <typename Kernel>
+void launch_persistent(Kernel kernel, size_t smem, LiftParams const &p,
+                       cudaStream_t s, int &per_sm, int &sms) {
   if (per_sm == 0) {
     if (smem > 0)
       cuda_check(cudaFuncSetAttribute(
@@ -35,7 +34,55 @@ void launch_r(LiftParams const &p, cudaStream_t s) {
   long long const resident = static_cast<long long>(per_sm) * sms;
   long long const blocks = std::min(p.total_tiles, resident);
   kernel<<<static_cast<unsigned>(blocks), kThreads, smem, s>>>(p);
-  cuda_check(cudaGetLastError(), "lift_kernel launch");
+  cuda_check(cudaGetLastError(), "lifting kernel launch");
+}
+
+template <class A, int R, class Sched, bool Direct>
+void launch_r(LiftParams const &p, cudaStream_t s) {
+  // Direct kernels keep pencils in registers and need no staging memory.
+  size_t const smem = Direct ? 0 : lift_smem_bytes<A, R, kThreads>(kRounds);
+  static thread_local int per_sm = 0;
+  static thread_local int sms = 0;
+  launch_persistent(lift_kernel<A, R, kThreads, Sched, Direct>, smem, p, s,
+                    per_sm, sms);
+}
+
+template <class A, int R, class Sched, bool Contig>
+void launch_wide_r(LiftParams const &p, cudaStream_t s) {
+  static thread_local int per_sm = 0;
+  static thread_local int sms = 0;
+  launch_persistent(wide_kernel<A, R, kThreads, Sched, Contig>,
+                    wide_smem_bytes<A, R, kThreads>(), p, s, per_sm, sms);
+}
+
+// Row policy A (arith.cuh), code kWide + R (strided axis) or kWideContig + R
+// (last axis) with R in {2, 4, 8, 16}; the wide kernel exists for the
+// wavelet schedules only.
+template <class A>
+void launch_wide(int sched, int code, LiftParams const &p, cudaStream_t s) {
+  auto by_r = [&](auto sch) {
+    using Sched = decltype(sch);
+    switch (code) {
+    case kWide + 2: return launch_wide_r<A, 2, Sched, false>(p, s);
+    case kWide + 4: return launch_wide_r<A, 4, Sched, false>(p, s);
+    case kWide + 8: return launch_wide_r<A, 8, Sched, false>(p, s);
+    case kWide + 16: return launch_wide_r<A, 16, Sched, false>(p, s);
+    case kWideContig + 2: return launch_wide_r<A, 2, Sched, true>(p, s);
+    case kWideContig + 4: return launch_wide_r<A, 4, Sched, true>(p, s);
+    case kWideContig + 8: return launch_wide_r<A, 8, Sched, true>(p, s);
+    case kWideContig + 16: return launch_wide_r<A, 16, Sched, true>(p, s);
+    }
+    throw StatusError(2, "bad chunk size");
+  };
+  switch (sched) {
+  case 0: return by_r(WaveletSched<0, false>{});
+  case 1: return by_r(WaveletSched<0, true>{});
+  case 2: return by_r(WaveletSched<1, false>{});
+  case 3: return by_r(WaveletSched<1, true>{});
+  case 4: return by_r(WaveletSched<2, false>{});
+  case 5: return by_r(WaveletSched<2, true>{});
+  }
+  throw StatusError(2, "wide kernel planned without a wavelet schedule");
 }
 
 // R > 0: staged tiles with chunks of R points; R < 0: direct pencils of
@@ -74,6 +121,10 @@ void launch_lift_f64(bool exact, int sched, int R, LiftParams const &p,
 void launch_lift_f32(bool exact, int sched, int R, LiftParams const &p,
                      cudaStream_t s);
 void launch_lift_f32c(bool exact_sym, int sched, int R, LiftParams const &p,
+                      cudaStream_t s);
+void launch_wide_f64(int sched, int code, LiftParams const &p, cudaStream_t s);
+void launch_wide_f32(int sched, int code, LiftParams const &p, cudaStream_t s);
+void launch_wide_f32c(int sched, int code, LiftParams const &p,
                       cudaStream_t s);
 
 } // namespace pgb

@@ -166,6 +166,19 @@ __device__ __forceinline__ DF shfl(DF x, int src) {
   return {__shfl_sync(0xffffffffu, x.h, src),
           __shfl_sync(0xffffffffu, x.l, src)};
 }
+// Rows of adjacent columns (the wide kernel's values).
+__device__ __forceinline__ f2 shfl(f2 x, int src) {
+  return __shfl_sync(0xffffffffu, x, src);
+}
+__device__ __forceinline__ DF2 shfl(DF2 x, int src) {
+  return {shfl(x.h, src), shfl(x.l, src)};
+}
+__device__ __forceinline__ F32Row4 shfl(F32Row4 x, int src) {
+  return {shfl(x.a, src), shfl(x.b, src)};
+}
+__device__ __forceinline__ F64Row2 shfl(F64Row2 x, int src) {
+  return {shfl(x.x, src), shfl(x.y, src)};
+}
 
 // Shared-memory staging layout of one tile: column w, chunk c, slot j at
 //   w * pitch + c * (R + 1) + j,   pitch = G * (R + 1) rounded up to odd.
@@ -178,28 +191,37 @@ __device__ __forceinline__ int stage_pitch(int G) {
 }
 
 // Exchanges between the chunks of one column during the level steps of a
-// round. Chunk c of a column is lane c of its group when G <= 32 (warp
-// shuffles); longer columns exchange through shared memory with one barrier
-// per step (the same for every thread of the CTA: G is uniform per tile).
+// round. When G <= 32 the chunks of a column are lanes of one warp and
+// exchange by shuffle: chunk c is lane (lane & ~mask) | (c << log2ls) with
+// mask = (G - 1) << log2ls, i.e. consecutive lanes (log2ls = 0) or lanes
+// 2^log2ls apart (the wide kernel, whose neighbouring lanes hold
+// neighbouring columns). Longer columns exchange through shared memory with
+// one barrier per step (the same for every thread of the CTA: G is uniform
+// per tile).
 template <class A, int NT> struct RoundCtx {
   using V = typename A::V;
-  int t, c, G, log2G, gbase_lane, periodic;
+  int t, c, G, log2G, log2ls, gbase_lane, periodic;
   V *heads, *xch;
   int buf = 0;
   bool heads_valid = false;
 
   __device__ __forceinline__ RoundCtx(int t_, int c_, int G_, int log2G_,
                                       int lane, int periodic_, V *heads_,
-                                      V *xch_)
-      : t(t_), c(c_), G(G_), log2G(log2G_), gbase_lane(lane & ~(G_ - 1)),
-        periodic(periodic_), heads(heads_), xch(xch_) {}
+                                      V *xch_, int log2ls_ = 0)
+      : t(t_), c(c_), G(G_), log2G(log2G_), log2ls(log2ls_),
+        gbase_lane(lane & ~((G_ - 1) << log2ls_)), periodic(periodic_),
+        heads(heads_), xch(xch_) {}
+
+  __device__ __forceinline__ int chunk_lane(int cc) const {
+    return gbase_lane | ((cc & (G - 1)) << log2ls);
+  }
 
   // The neighbour of a fine step: slot 0 of the next chunk (o = 1) or slot
   // R - s of the previous chunk (o = 0); `pub` is this chunk's value of it.
   __device__ __forceinline__ V fine_neighbor(int o, V pub) {
     if (G == 1) return pub;
     int nc = (o == 1) ? c + 1 : c - 1;
-    if (G <= 32) return shfl(pub, gbase_lane | (nc & (G - 1)));
+    if (G <= 32) return shfl(pub, chunk_lane(nc));
     xch[buf * NT + t] = pub;
     __syncthreads();
     if (periodic)
@@ -219,8 +241,8 @@ template <class A, int NT> struct RoundCtx {
   __device__ __forceinline__ void coarse(V &v0, int o, int d, Upd upd) {
     bool const mine = (c & (2 * d - 1)) == o * d;
     if (G <= 32) {
-      V const lo = shfl(v0, gbase_lane | ((c - d) & (G - 1)));
-      V const up = shfl(v0, gbase_lane | ((c + d) & (G - 1)));
+      V const lo = shfl(v0, chunk_lane(c - d));
+      V const up = shfl(v0, chunk_lane(c + d));
       if (mine) v0 = upd(lo, v0, up);
       return;
     }
@@ -489,8 +511,15 @@ template <int W, bool FWD> struct WaveletSched {
                                              RoundCtx<A, NT> &ctx,
                                              LiftJob const &job,
                                              LiftParams const &) {
+    run_levels<A, R, NT>(v, ctx, job.nlevels);
+  }
+
+  // The L levels of a job (shifts 0 .. L-1 forward, L-1 .. 0 inverse).
+  template <class A, int R, int NT>
+  static __device__ __forceinline__ void run_levels(typename A::V (&v)[R],
+                                                    RoundCtx<A, NT> &ctx,
+                                                    int L) {
     constexpr int LOG2R = Log2<R>::value;
-    int const L = job.nlevels;
     if constexpr (A::kPacked && R >= 4) {
       constexpr int H = R / 2;
       DF2 q[H];
@@ -525,8 +554,10 @@ template <int W, bool FWD> struct WaveletSched {
   }
 };
 
-// Asynchronous 4- or 8-byte copy from global to shared memory (sm_80+):
-// loads stay in flight without occupying registers.
+// Asynchronous 4-, 8- or 16-byte copy from global to shared memory (sm_80+):
+// loads stay in flight without occupying registers. The copies go through
+// L1 (.ca): a warp's copies often cover only part of each 32-byte sector,
+// and the rest of the sector is read by the next copy instructions.
 template <int BYTES>
 __device__ __forceinline__ void cp_async(void *smem, void const *gmem) {
   unsigned const dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));
@@ -536,6 +567,13 @@ __device__ __forceinline__ void cp_async(void *smem, void const *gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// Waits until at most N of this thread's most recent groups are in flight.
+template <int N> __device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 // R values of one pencil: 16-byte vectors when contiguous and aligned,
@@ -739,6 +777,30 @@ template <typename S, int R, int NT> struct TileCopy {
 // by one thread (no staging); otherwise tiles are staged through shared
 // memory. The two paths are separate instantiations so that neither's
 // register budget constrains the other.
+// Moves the job cursor `ji` forward to the job of `tile` and copies that job
+// into shared memory when it changed. Called by every thread of the CTA.
+// The current job lives in shared memory: its fields are read in the inner
+// loops, and a generic pointer into parameter or global space would turn
+// every read into a memory instruction.
+template <int NT>
+__device__ __forceinline__ void fetch_job(LiftParams const &p, long long tile,
+                                          int t, int &ji, LiftJob &sjob,
+                                          int &sjob_index) {
+  if (p.jobs != nullptr)
+    while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
+  if (sjob_index != ji) {
+    __syncthreads();  // every thread has read sjob_index
+    constexpr int WORDS = sizeof(LiftJob) / 4;
+    static_assert(sizeof(LiftJob) % 4 == 0, "LiftJob is copied in words");
+    unsigned const *src = reinterpret_cast<unsigned const *>(
+        p.jobs != nullptr ? p.jobs + ji : &p.job);
+    for (int i = t; i < WORDS; i += NT)
+      reinterpret_cast<unsigned *>(&sjob)[i] = src[i];
+    if (t == 0) sjob_index = ji;
+    __syncthreads();
+  }
+}
+
 template <class A, int R, int NT, class Sched, bool Direct>
 __global__ void __launch_bounds__(NT)
     lift_kernel(__grid_constant__ const LiftParams p) {
@@ -753,9 +815,6 @@ __global__ void __launch_bounds__(NT)
 
   int const t = threadIdx.x;
   int const lane = t & 31;
-  // The current job lives in shared memory: its fields are read in the inner
-  // loops, and a generic pointer into parameter or global space would turn
-  // every read into a memory instruction.
   __shared__ LiftJob sjob;
   __shared__ int sjob_index;
   LiftJob const *const job = &sjob;
@@ -764,20 +823,8 @@ __global__ void __launch_bounds__(NT)
   // Persistent CTAs: tiles are visited in increasing order, so the job
   // cursor only moves forward.
   for (long long tile = blockIdx.x; tile < p.total_tiles; tile += gridDim.x) {
-    if (p.jobs != nullptr)
-      while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
     __syncthreads();  // the previous tile is out of shared memory
-    if (sjob_index != ji) {
-      __syncthreads();  // every thread has read sjob_index
-      constexpr int WORDS = sizeof(LiftJob) / 4;
-      static_assert(sizeof(LiftJob) % 4 == 0, "LiftJob is copied in words");
-      unsigned const *src = reinterpret_cast<unsigned const *>(
-          p.jobs != nullptr ? p.jobs + ji : &p.job);
-      for (int i = t; i < WORDS; i += NT)
-        reinterpret_cast<unsigned *>(&sjob)[i] = src[i];
-      if (t == 0) sjob_index = ji;
-      __syncthreads();
-    }
+    fetch_job<NT>(p, tile, t, ji, sjob, sjob_index);
     int const log2W = job->log2_window;       // points per column held
     int const log2G = log2W - LOG2R;          // chunks per column
     int const G = 1 << log2G;
@@ -868,6 +915,292 @@ __global__ void __launch_bounds__(NT)
     cp.template run<true>(stage, t, seg, job->halo, job->seg_len);
     }
   }
+}
+
+// Wide kernel: each thread holds the same chunk of R points of kCols
+// adjacent pencils in registers (A::V is one row of them: the kCols points at
+// the same pencil position), for two layouts:
+//
+//  * strided axes (Contig = false) whose inner extent is at least kCols,
+//    pencils of up to 64 points: the G = n / R <= 4 chunks of a pencil are
+//    lanes 32 / G apart, so the lanes of one warp that hold the same chunk
+//    hold consecutive column groups and every row a warp reads is
+//    32 / G * kCols contiguous elements;
+//  * the last axis (Contig = true), pencils of up to 512 points: a thread's
+//    chunk of each of its kCols pencils is R contiguous points, and the
+//    G = n / R <= 32 chunks of a pencil group are consecutive lanes, so a
+//    warp reads whole runs of consecutive pencils.
+//
+// Chunks exchange by shuffle; there is no barrier. A CTA takes a contiguous
+// range of tiles (a tile is kTileRounds units; a unit is NT / G column groups
+// of kCols columns). Loads are software pipelined: each thread copies the
+// data of the unit WideStages - 1 ahead with cp.async into its own
+// shared-memory slots while it transforms the current unit, whose data it
+// then reads from those slots; results are stored straight to global memory.
+template <class A> struct WideStages {
+  static constexpr int value = sizeof(typename A::Store) == 16 ? 2 : 3;
+};
+
+// Geometry of one unit for one thread.
+struct WideUnit {
+  long long off;  // element offset of the thread's chunk of its first column
+  long long wfirst;  // first column group of the warp
+  long long groups;  // column groups of the job
+  int c;          // chunk index
+  int log2ls;     // log2 of the lane distance between chunks of a column
+  bool active;    // the warp has at least one column group in range
+  bool keep;      // the thread's column group is in range (else recomputed)
+};
+
+template <int LOG2R, int LOG2NT, int LOG2CW, bool Contig>
+__device__ __forceinline__ WideUnit wide_unit(LiftJob const &job,
+                                              long long unit, int t) {
+  int const lane = t & 31;
+  int const log2G = job.log2_n - LOG2R;
+  int const log2gw = 5 - log2G;  // column groups per warp
+  int const log2CR = LOG2NT - log2G;
+  long long const tile = unit / kTileRounds;
+  int const r = static_cast<int>(unit - tile * kTileRounds);
+  long long const groups = job.columns >> LOG2CW;
+  long long const wfirst =
+      (tile - job.tile_begin) * (static_cast<long long>(kTileRounds)
+                                 << log2CR) +
+      (r << log2CR) + (static_cast<long long>(t >> 5) << log2gw);
+  WideUnit w;
+  w.wfirst = wfirst;
+  w.groups = groups;
+  w.active = wfirst < groups;
+  int gl;  // column group within the warp
+  if (Contig) {
+    w.c = lane & ((1 << log2G) - 1);
+    gl = lane >> log2G;
+    w.log2ls = 0;
+  } else {
+    w.c = lane >> log2gw;
+    gl = lane & ((1 << log2gw) - 1);
+    w.log2ls = log2gw;
+  }
+  long long gg = wfirst + gl;
+  w.keep = gg < groups;
+  if (!w.keep) gg = groups - 1;
+  long long const gc = gg << LOG2CW;  // first column of the group
+  int const log2B = job.log2_inner;
+  w.off = ((gc >> log2B) << job.log2_astride) + (gc & ((1LL << log2B) - 1)) +
+          (static_cast<long long>(w.c) << (LOG2R + job.log2_kstride));
+  return w;
+}
+
+// Last job whose first tile is <= tile (jobs sorted by tile_begin).
+__device__ __forceinline__ int find_job(LiftParams const &p, long long tile) {
+  int lo = 0, hi = p.njobs - 1;
+  while (lo < hi) {
+    int const mid = (lo + hi + 1) >> 1;
+    if (p.jobs[mid].tile_begin <= tile)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Contiguous layout: the thread's elements e = k * R + j (column k, point j)
+// in 16-byte pieces; piece i starts at element i * PER, which lies at
+// k * n + j from the thread's offset (a piece never crosses a column: R is a
+// multiple of PER, or the kCols chunks are whole adjacent pencils, n == R).
+template <class A, int R> struct ContigPieces {
+  using E = typename A::Elem;
+  static constexpr int PER = 16 / sizeof(E);
+  static constexpr int LOG2PER = Log2<PER>::value;
+  static constexpr int N = A::kCols * R / PER;
+  static constexpr int LOG2N = Log2<N>::value;
+  static_assert(A::kCols * R % PER == 0, "whole 16-byte pieces");
+  static __device__ __forceinline__ long long at(int i, int log2_n) {
+    int const e = i * PER;
+    return (static_cast<long long>(e / R) << log2_n) + e % R;
+  }
+  // The pencils of one warp are one contiguous block of 32 * N pieces that
+  // the lanes copy in order (coalesced). Piece b of the block belongs to
+  // lane `owner` as its piece p.
+  static __device__ __forceinline__ void owner_of(int b, int log2_n,
+                                                  int &owner, int &p) {
+    constexpr int LOG2CW = Log2<A::kCols>::value;
+    constexpr int LOG2R = Log2<R>::value;
+    // One chunk per pencil (always so when a chunk is shorter than a
+    // piece): each lane's N pieces are consecutive.
+    if (R < PER || log2_n == LOG2R) {
+      owner = b >> LOG2N;
+      p = b & (N - 1);
+      return;
+    }
+    if constexpr (R >= PER) {
+      int const o = b << LOG2PER;
+      int const pk = o >> log2_n;  // pencil in the block
+      int const point = o & ((1 << log2_n) - 1);
+      int const log2G = log2_n - LOG2R;
+      owner = ((pk >> LOG2CW) << log2G) | (point >> LOG2R);
+      p = ((pk & (A::kCols - 1)) << (LOG2R - LOG2PER)) |
+          ((point & (R - 1)) >> LOG2PER);
+    }
+  }
+  // Slot of lane's piece p among the warp's 32 * N slots: lane-major with a
+  // rotation that puts the same piece of 8 consecutive lanes in 8 distinct
+  // 16-byte bank groups (conflict-free reads).
+  static __device__ __forceinline__ int slot(int lane, int p) {
+    constexpr int SH = LOG2N >= 3 ? 0 : 3 - LOG2N;
+    return (lane << LOG2N) + ((p + (lane >> SH)) & (N - 1));
+  }
+};
+
+template <class A, int R, int NT, class Sched, bool Contig>
+__global__ void __launch_bounds__(NT)
+    wide_kernel(__grid_constant__ const LiftParams p) {
+  using V = typename A::V;
+  using W = typename A::Store;
+  using E = typename A::Elem;
+  using CP = ContigPieces<A, R>;
+  constexpr int CW = A::kCols;
+  constexpr int LOG2CW = Log2<CW>::value;
+  constexpr int LOG2R = Log2<R>::value;
+  constexpr int LOG2NT = Log2<NT>::value;
+  constexpr int S = WideStages<A>::value;
+  static_assert(sizeof(W) == CW * sizeof(E), "row vector size");
+  static_assert(R * sizeof(W) % 16 == 0, "slots of whole 16-byte pieces");
+  // Per stage R * NT rows of W (strided) or CP::N * NT pieces (contiguous):
+  // the same bytes, slot-major so that a warp's slots are consecutive.
+  constexpr int SLOT_BYTES = R * sizeof(W);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+
+  int const t = threadIdx.x;
+  int const lane = t & 31;
+  long long const T = p.total_tiles;
+  long long const u0 = T * blockIdx.x / gridDim.x * kTileRounds;
+  long long const u1 = T * (blockIdx.x + 1) / gridDim.x * kTileRounds;
+  if (u0 >= u1) return;
+  bool const many = p.jobs != nullptr;
+  // Job cursors of the copy stream and of the compute stream: both only
+  // move forward through the CTA's contiguous range.
+  int jl = many ? find_job(p, u0 / kTileRounds) : 0;
+  int jc = jl;
+  auto job_of = [&](int &ji, long long unit) -> LiftJob const & {
+    if (!many) return p.job;
+    long long const tile = unit / kTileRounds;
+    while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
+    return p.jobs[ji];
+  };
+  auto stage_base = [&](long long unit) {
+    return smem_raw + static_cast<int>(unit % S) * (SLOT_BYTES * NT);
+  };
+  auto prefetch = [&](long long unit) {
+    LiftJob const &job = job_of(jl, unit);
+    WideUnit const w =
+        wide_unit<LOG2R, LOG2NT, LOG2CW, Contig>(job, unit, t);
+    if (w.active) {
+      unsigned char *const st = stage_base(unit);
+      if constexpr (Contig) {
+        // Lanes copy consecutive pieces of the warp's block; pieces of
+        // lanes past the last column group come from the last group.
+        int const log2blk = LOG2CW + job.log2_n;  // elements per group
+        E const *const wsrc = reinterpret_cast<E const *>(job.base) +
+                              (w.wfirst << log2blk);
+        uint4 *const wslots =
+            reinterpret_cast<uint4 *>(st) + (t & ~31) * CP::N;
+#pragma unroll
+        for (int i = 0; i < CP::N; ++i) {
+          int const b = i * 32 + lane;
+          int owner, pc;
+          CP::owner_of(b, job.log2_n, owner, pc);
+          long long o = static_cast<long long>(b) << CP::LOG2PER;
+          long long const over =
+              w.wfirst + (o >> log2blk) - (w.groups - 1);
+          if (over > 0) o -= over << log2blk;
+          cp_async<16>(wslots + CP::slot(owner, pc), wsrc + o);
+        }
+      } else {
+        E const *const src = reinterpret_cast<E const *>(job.base) + w.off;
+        W *const dst = reinterpret_cast<W *>(st) + t;
+        long long const kstride = 1LL << job.log2_kstride;
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+          cp_async<sizeof(W)>(dst + j * NT, src + j * kstride);
+      }
+    }
+    cp_async_commit();
+  };
+
+#pragma unroll
+  for (int k = 0; k < S - 1; ++k)
+    if (u0 + k < u1) prefetch(u0 + k); else cp_async_commit();
+  for (long long u = u0; u < u1; ++u) {
+    // Contiguous layout: lanes copy into each other's slots, so every lane
+    // must be done reading the stage that the next prefetch overwrites, and
+    // must see the other lanes' copies of unit u.
+    if constexpr (Contig) __syncwarp();
+    if (u + S - 1 < u1) prefetch(u + S - 1); else cp_async_commit();
+    cp_async_wait_group<S - 1>();  // this thread's copies of unit u are in
+    if constexpr (Contig) __syncwarp();
+    LiftJob const &job = job_of(jc, u);
+    WideUnit const w = wide_unit<LOG2R, LOG2NT, LOG2CW, Contig>(job, u, t);
+    if (!w.active) continue;  // the whole warp
+    unsigned char const *const st = stage_base(u);
+    V v[R];
+    if constexpr (Contig) {
+      E el[CW * R];
+      uint4 const *const wslots =
+          reinterpret_cast<uint4 const *>(st) + (t & ~31) * CP::N;
+#pragma unroll
+      for (int i = 0; i < CP::N; ++i) {
+        uint4 const q = wslots[CP::slot(lane, i)];
+        memcpy(el + i * CP::PER, &q, 16);
+      }
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        E row[CW];
+#pragma unroll
+        for (int k = 0; k < CW; ++k) row[k] = el[k * R + j];
+        W x;
+        memcpy(&x, row, sizeof(W));
+        v[j] = A::load(x);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < R; ++j)
+        v[j] = A::load(reinterpret_cast<W const *>(st)[j * NT + t]);
+    }
+    int const log2G = job.log2_n - LOG2R;
+    RoundCtx<A, NT> ctx(t, w.c, 1 << log2G, log2G, lane, 1, nullptr, nullptr,
+                        w.log2ls);
+    Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
+    if (w.keep) {
+      E *const dst = reinterpret_cast<E *>(job.dst_base) + w.off;
+      if constexpr (Contig) {
+        E el[CW * R];
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+          W const x = A::store(v[j]);
+          E row[CW];
+          memcpy(row, &x, sizeof(W));
+#pragma unroll
+          for (int k = 0; k < CW; ++k) el[k * R + j] = row[k];
+        }
+#pragma unroll
+        for (int i = 0; i < CP::N; ++i) {
+          uint4 q;
+          memcpy(&q, el + i * CP::PER, 16);
+          *reinterpret_cast<uint4 *>(dst + CP::at(i, job.log2_n)) = q;
+        }
+      } else {
+        long long const kstride = 1LL << job.log2_kstride;
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+          *reinterpret_cast<W *>(dst + j * kstride) = A::store(v[j]);
+      }
+    }
+  }
+  cp_async_wait_all();
+}
+
+template <class A, int R, int NT> constexpr size_t wide_smem_bytes() {
+  return size_t(WideStages<A>::value) * R * NT * sizeof(typename A::Store);
 }
 
 // Dynamic shared memory of one CTA (an upper bound over every column shape:

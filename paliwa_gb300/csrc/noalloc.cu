@@ -98,7 +98,7 @@ extern "C" int paliwa_gb_transform_noalloc(void *grid, int dtype, int ndim,
     std::vector<std::vector<Stage>> plans(ndim);
     for (int d = 0; d < ndim; ++d) {
       AxisView view = axis_view(reinterpret_cast<unsigned long long>(grid),
-                                ndim, level, d);
+                                ndim, level, d, dtype);
       auto const shifts = level_shifts(level[d], minimum_level[d], forward);
       if (needs_shadow(view, shifts)) {
         if (grid_bytes(dtype, ndim, level) > kStaticScratchBytes)

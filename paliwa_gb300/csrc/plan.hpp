@@ -46,14 +46,26 @@ struct AxisView {
   int log2_kstride = 0;  // element stride between consecutive pencil points
   int log2_astride = 0;  // element stride between consecutive outer indices
   int log2_n = 0;        // pencil length
+  // log2 of the adjacent columns one thread of the wide kernel holds for this
+  // grid's storage type (0: the grid is not aligned to such a row).
+  int log2_row = 0;
+  // The wide kernel also takes the last axis (FP32 compensated only: plain
+  // FP32 and FP64 run faster there on the direct kernel, which needs fewer
+  // registers per pencil).
+  bool wide_last = false;
 };
 
 AxisView axis_view(unsigned long long base, int ndim, int64_t const *level,
-                   int dim);
+                   int dim, int dtype);
 
-// One stage of an axis transform: a job for a kernel with chunk size R. The
-// stages of one axis must run in order; stages of different grids are
-// independent.
+// Stage::R names the kernel and its chunk size: R > 0 the staged kernel with
+// chunks of R points, -R the direct kernel, kWide + R the wide kernel on a
+// strided axis, kWideContig + R the wide kernel on the last axis.
+constexpr int kWide = 64;
+constexpr int kWideContig = 128;
+
+// One stage of an axis transform: a job for one kernel. The stages of one
+// axis must run in order; stages of different grids are independent.
 struct Stage {
   int R = 0;
   long long tiles = 0;

@@ -68,6 +68,17 @@ def packed_grids(levels, dtype, device="cuda", align=64):
     return buf, [buf.narrow(0, o, s) for o, s in zip(offsets, sizes)]
 
 
+def kernel_name(code):
+    """Name of the lifting kernel behind a launch code of Batch.profile."""
+    if code > 128:
+        return f"wide_kernel last axis R={code - 128}"
+    if code > 64:
+        return f"wide_kernel R={code - 64}"
+    if code < 0:
+        return f"lift_kernel direct R={-code}"
+    return f"lift_kernel staged R={code}"
+
+
 def _ptr_array(grids):
     arr = (ctypes.c_void_p * len(grids))()
     for i, g in enumerate(grids):
@@ -128,17 +139,20 @@ class Batch:
         return f.value, i.value
 
     def profile(self, forward=True, stream=None):
-        """Per-launch (milliseconds, algorithmic bytes) of one direction,
-        launched without a graph and bracketed by CUDA events."""
+        """Per-launch (milliseconds, algorithmic bytes, kernel) of one
+        direction, launched without a graph and bracketed by CUDA events.
+        kernel: R > 0 staged with chunks of R points, -R direct, 64 + R
+        wide (see :func:`kernel_name`)."""
         n = ctypes.c_int()
         s = _stream_handle(self.grids[0], stream)
         _lib.check(self._lib.paliwa_gb_batch_profile(
-            self._h, int(forward), s, 0, ctypes.byref(n), None, None))
+            self._h, int(forward), s, 0, ctypes.byref(n), None, None, None))
         ms = (ctypes.c_float * max(1, n.value))()
         by = (ctypes.c_int64 * max(1, n.value))()
+        kd = (ctypes.c_int32 * max(1, n.value))()
         _lib.check(self._lib.paliwa_gb_batch_profile(
-            self._h, int(forward), s, n.value, ctypes.byref(n), ms, by))
-        return list(ms[:n.value]), list(by[:n.value])
+            self._h, int(forward), s, n.value, ctypes.byref(n), ms, by, kd))
+        return (list(ms[:n.value]), list(by[:n.value]), list(kd[:n.value]))
 
     def close(self):
         if self._h:

@@ -230,3 +230,38 @@ def test_full_scheme_batch_deterministic_and_exact():
     s.synchronize()
     assert torch.max(torch.abs(buf - pristine)) <= 1e-12
     b.close()
+
+
+def test_batch_compensated_bit_exact_model():
+    """FP32-compensated batch of a whole 4D scheme (|l|_1 = 14 - q, 791
+    grids of uneven shapes, one job list per launch): every kernel variant
+    the plan picks, bit for bit against the numpy model of the compensated
+    arithmetic, forward and inverse."""
+    import torch
+    from compensated import hierarchize as model
+    levels, _ = pct.combination_scheme(4, 14, 3, 1)
+    lmin, lmax = (1, 1, 1, 1), (11, 11, 11, 11)
+    rng = np.random.default_rng(11)
+    buf, gs = pct.packed_grids(levels, torch.float32)
+    buf.copy_(torch.from_numpy(rng.uniform(-1, 1, buf.numel())))
+    pristine = buf.cpu().numpy().copy()
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    b = pct.Batch(gs, levels, lmin, lmax, "biorthogonal", compensated=True)
+    base = buf.data_ptr() // 4
+    for forward in (True, False):
+        buf.copy_(torch.from_numpy(pristine))
+        torch.cuda.synchronize()
+        (b.hierarchize if forward else b.dehierarchize)(s)
+        s.synchronize()
+        out = buf.cpu().numpy()
+        for i in range(0, len(levels), 3):
+            lv = levels[i]
+            o = gs[i].data_ptr() // 4 - base
+            shape = [1 << l for l in lv]
+            x = pristine[o:o + gs[i].numel()].reshape(shape)
+            want = model(x, lv, lmin, "biorthogonal", forward)
+            got = out[o:o + gs[i].numel()].reshape(shape)
+            assert np.array_equal(got.view(np.uint32),
+                                  want.view(np.uint32)), (lv, forward)
+    b.close()

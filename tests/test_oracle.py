@@ -112,3 +112,26 @@ def test_oracle_errors(oracle_mod):
         oracle_mod.hierarchize(x, (2, 2), (3, 0), (2, 2), "hat")
     with pytest.raises(RuntimeError):  # paliwa_transform.hpp:239-240
         oracle_mod.transform_in(x, (2, 2), (2, 2), 0, [2], [(2, (0, 1, 0))])
+
+
+@pytest.mark.parametrize("wavelet", ["hat", "biorthogonal", "fullweighting"])
+def test_compensated_model_close_to_fp64(oracle_mod, wavelet):
+    """The FP32-compensated model stays within 1e-6 (normwise max) of the
+    FP64 oracle on the same FP32 inputs, and well inside plain FP32's error:
+    it is a faithful model of a compensated scheme, not of plain FP32."""
+    from compensated import hierarchize as model
+    level, lmin = (6, 5, 4), (0, 1, 0)
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1.0, 1.0, [1 << l for l in level]).astype(np.float32)
+    for forward in (True, False):
+        ref = oracle_mod.hierarchize(x.astype(np.float64), level, lmin, level,
+                                     wavelet, forward=forward)
+        got = model(x, level, lmin, wavelet, forward).astype(np.float64)
+        plain = oracle_mod.hierarchize(x.copy(), level, lmin, level, wavelet,
+                                       forward=forward).astype(np.float64)
+        scale = np.max(np.abs(ref))
+        err = np.max(np.abs(got - ref)) / scale
+        err_plain = np.max(np.abs(plain - ref)) / scale
+        assert err <= 1e-6, err
+        # One rounding per axis and point: at most 3 ulps-scale errors.
+        assert err <= 3 * 2.0 ** -24 * 1.01 + 1e-12 or err < err_plain

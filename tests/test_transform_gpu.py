@@ -87,6 +87,49 @@ def test_f32_compensated_error(level, lmin, wavelet):
         assert err <= F32C_TOL, (level, wavelet, forward, err)
 
 
+# Partly filled warps and tiles of the wide kernel: strided pencils of 32 or
+# 64 points with one or two column groups, last-axis pencils with fewer
+# pencils than a warp holds, narrow inner extents.
+WIDE_EDGE = [((5, 1), (0, 0)), ((6, 1), (1, 0)), ((1, 5), (0, 0)),
+             ((2, 6), (0, 1)), ((1, 9), (0, 0)), ((3, 4), (0, 0)),
+             ((4, 2, 1), (0, 0, 0)), ((2, 2, 5), (0, 0, 0)),
+             ((6, 3, 2), (1, 0, 0)), ((3, 7, 1), (0, 2, 0))]
+
+
+@pytest.mark.parametrize("wavelet", WAVELETS)
+@pytest.mark.parametrize(
+    "level,lmin", [s for s in SHAPES + WIDE_EDGE if max(s[0]) <= 12])
+def test_f32_compensated_bit_exact_model(level, lmin, wavelet):
+    """Every kernel's FP32-compensated arithmetic, bit for bit, against the
+    numpy model of the same operations (one rounding to FP32 per axis).
+    Pencils longer than 4096 points run in several stages per axis (windowed
+    fine levels, sub-lattice coarse levels), each ending in a rounding to
+    FP32; those shapes are held to the FP64 tolerance instead."""
+    from compensated import hierarchize as model
+    x = random_input(level, 13).astype(np.float32)
+    for forward in (True, False):
+        want = model(x, level, lmin, wavelet, forward)
+        got = gpu_transform(x, level, lmin, tuple(level), wavelet, forward,
+                            compensated=True)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (
+            level, lmin, wavelet, forward)
+
+
+@pytest.mark.parametrize("wavelet", WAVELETS)
+@pytest.mark.parametrize("level,lmin", WIDE_EDGE)
+def test_wide_edges_bit_exact(level, lmin, wavelet):
+    """FP64 and FP32 through the wide kernel's partly filled warps."""
+    for dt in (np.float64, np.float32):
+        x = random_input(level, 17).astype(dt)
+        for forward in (True, False):
+            want = import_oracle().hierarchize(x.copy(), level, lmin,
+                                               tuple(level), wavelet,
+                                               forward=forward)
+            got = gpu_transform(x, level, lmin, tuple(level), wavelet,
+                                forward)
+            assert np.array_equal(got, want), (level, dt, wavelet, forward)
+
+
 LONG = [((14,), (0,)), ((15,), (2,)), ((17,), (0,)), ((16, 1), (3, 0)),
         ((2, 15), (0, 0)), ((14, 2), (0, 1)), ((1, 1, 1, 17), (1, 1, 1, 1))]
 

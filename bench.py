@@ -57,6 +57,10 @@ WORKLOADS = {
                      wavelet="biorthogonal", config_id=4),
     "6d-ct-16": dict(kind="ct", ndim=6, level_sum=16, qmax=5, lmin=1,
                      wavelet="biorthogonal", config_id=5),
+    # The 4D scheme at |l|_1 = 16 - q (1325 grids, 48 M points): the same
+    # kernels on a few GB of device memory, for profiler captures.
+    "4d-ct-16": dict(kind="ct", ndim=4, level_sum=16, qmax=3, lmin=1,
+                     wavelet="biorthogonal", config_id=4),
     "3d-biorthogonal-999": dict(kind="grid", level=(9, 9, 9), lmin=(0, 0, 0),
                                 wavelet="biorthogonal", config_id=2),
     "6d-hat-555544": dict(kind="grid", level=(5, 5, 5, 5, 4, 4),
@@ -307,6 +311,25 @@ def run_reference(args, w, world, rank):
 # GPU
 
 
+DRAM_RATIO_FILE = "profiles/lift_kernels_4d_ct_20_dram_ratio.txt"
+
+
+def dram_ratio(kernel):
+    """DRAM bytes per algorithmic byte of `kernel` (a name of
+    paliwa_gb300.ct.kernel_name) as measured by ncu on the 4d-ct-20 workload
+    and committed as 'name = ratio' lines; None when not measured."""
+    path = os.path.join(ROOT, DRAM_RATIO_FILE)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if "=" in line and not line.startswith("#"):
+                name, val = line.rsplit("=", 1)
+                if name.strip() == kernel:
+                    return float(val)
+    return None
+
+
 def upload_inputs(w, dev):
     """Packed device buffers (float64 and float32) of every grid, and a
     pristine float64 copy for accuracy checks."""
@@ -460,6 +483,13 @@ def run_gpu(args, w, world, rank, local):
             for fwd in (True, False):
                 ms, by, kd = bt.profile(fwd, stream)
                 rows += list(zip(ms, by, kd))
+                if args.launch_table and rank == 0:
+                    # The plan's launches in launch order (the order a
+                    # profiler lists them in): kernel, algorithmic bytes.
+                    for i, (m, b, k) in enumerate(zip(ms, by, kd)):
+                        print(f"launch {name} {'fwd' if fwd else 'inv'} "
+                              f"{i:3d} {pct.kernel_name(k):28s} {b:13d} B "
+                              f"{m:8.3f} ms", file=sys.stderr)
             prof[name] = rows
         nlaunch = sum(bt32.launches())
 
@@ -471,26 +501,39 @@ def run_gpu(args, w, world, rank, local):
     peak, peak_kind = peaks()
 
     def by_kernel(rows, peak):
-        """Time share and HBM fraction of each kernel over one step."""
+        """Launches, time share, algorithmic bytes and HBM fraction of each
+        kernel over one step."""
         out = {}
         tot = sum(r[0] for r in rows)
         for ms, by, code in rows:
-            k = out.setdefault(pct.kernel_name(code), [0.0, 0])
-            k[0] += ms
-            k[1] += by
-        return {name: {"share": ms / tot,
+            k = out.setdefault(pct.kernel_name(code), [0, 0.0, 0])
+            k[0] += 1
+            k[1] += ms
+            k[2] += by
+        return {name: {"launches": n, "share": ms / tot, "bytes": by,
                        "frac": by / (ms / 1e3) / 1e9 / peak}
-                for name, (ms, by) in sorted(out.items())}
+                for name, (n, ms, by) in sorted(out.items())}
 
     def roof(rows):
-        top = max(rows, key=lambda r: r[0])
+        """The kernel with the largest share of a step's time: its name,
+        launches, summed milliseconds and algorithmic bytes; and totals."""
+        per = {}
+        for ms, by, code in rows:
+            k = per.setdefault(pct.kernel_name(code), [0, 0.0, 0])
+            k[0] += 1
+            k[1] += ms
+            k[2] += by
+        name = max(per, key=lambda n: per[n][1])
         tot_ms = sum(r[0] for r in rows)
         tot_b = sum(r[1] for r in rows)
-        return top, tot_ms, tot_b
+        return (name, *per[name]), tot_ms, tot_b
 
     top32, tot32_ms, tot32_b = roof(prof["f32c"])
     top64, tot64_ms, tot64_b = roof(prof["f64"])
-    achieved = top32[1] / (top32[0] / 1e3) / 1e9
+    top_name, top_n, top_ms, top_b = top32
+    achieved = top_b / (top_ms / 1e3) / 1e9
+    ratio = dram_ratio(top_name)
+    traffic = None if ratio is None else ratio * top_b / top_n
 
     # End to end through the public API with pinned host buffers.
     host_in = torch.empty(b32.numel(), dtype=torch.float32).pin_memory()
@@ -538,12 +581,17 @@ def run_gpu(args, w, world, rank, local):
             "error_f32c_vs_f64": err,
             "roofline": {
                 "bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "traffic_source": None if ratio is None else
+                    "DRAM bytes / algorithmic bytes of this kernel from the "
+                    "ncu capture in " + DRAM_RATIO_FILE + ", times this "
+                    "run's algorithmic bytes per launch",
                 "peak_kind": peak_kind,
-                "kernel": pct.kernel_name(top32[2]) + ", FP32c (largest "
-                          "launch)",
+                "kernel": top_name + ", FP32c (largest share of the step)",
+                "launches_per_step": top_n,
                 "by_kernel": by_kernel(prof["f32c"], peak),
-                "bytes_per_launch": top32[1], "launch_ms": top32[0],
+                "bytes_per_launch": top_b / top_n,
+                "launch_ms": top_ms / top_n,
                 "all_launches_frac":
                     tot32_b / (tot32_ms / 1e3) / 1e9 / peak},
             "combine": combine,
@@ -569,6 +617,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline leg")
+    ap.add_argument("--launch-table", action="store_true",
+                    help="print the plan's launches (kernel, algorithmic "
+                         "bytes, event-timed ms) to stderr")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()

@@ -90,6 +90,7 @@ AxisView axis_view(unsigned long long base, int ndim, int64_t const *level,
   int const log2_row = dtype == PALIWA_GB_F32 ? 2 : 1;
   v.log2_row = (base % 16) == 0 ? log2_row : 0;
   v.wide_last = dtype == PALIWA_GB_F32C;
+  v.log2_es = dtype == PALIWA_GB_F64 ? 3 : 2;
   int log2_outer = 0, log2_inner = 0;
   for (int d = 0; d < dim; ++d) log2_outer += static_cast<int>(level[d]);
   for (int d = dim + 1; d < ndim; ++d) log2_inner += static_cast<int>(level[d]);
@@ -192,7 +193,18 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
     bool const wide_last = canon && last && v.wide_last && log2G <= 5 &&
                            v.columns >= (1LL << v.log2_row);
     bool const direct = R == (1 << v.log2_n) || (last && log2G <= 5);
-    if (wide) {
+    // Strided pencils of 128 to 512 points (256 with 8-byte row vectors,
+    // whose chunk padding would break 16-byte alignment at G = 32) whose
+    // inner extent holds whole 16-byte pieces run on the tile kernel.
+    int const log2_row_bytes = v.log2_row + v.log2_es;
+    bool const tile = canon && !last && R == 16 && log2G >= 3 &&
+                      log2G <= (log2_row_bytes == 4 ? 5 : 4) &&
+                      v.log2_inner + v.log2_es >= 4;
+    if (tile) {
+      st.R = kTile + 16;
+      st.job.col_tiles =
+          ceil_div(v.columns >> v.log2_row, kThreads >> log2G);
+    } else if (wide) {
       st.R = kWide + wR;
       st.job.col_tiles = ceil_div(v.columns >> v.log2_row, wC);
     } else if (wide_last) {
@@ -339,7 +351,7 @@ void launch_lift(int dtype, bool exact, bool symmetric, int sched, int R,
   params.total_tiles = total_tiles;
   params.rounds = kRounds;
   if (params.fp64_log2_points >= 0) sched = -1;
-  if (R > kWide) {  // both layouts of the wide kernel
+  if (R > kWide) {  // the wide and tile kernels
     switch (dtype) {
     case PALIWA_GB_F64: return launch_wide_f64(sched, R, params, s);
     case PALIWA_GB_F32: return launch_wide_f32(sched, R, params, s);

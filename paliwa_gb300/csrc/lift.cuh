@@ -1052,7 +1052,7 @@ template <class A, int R> struct ContigPieces {
 };
 
 template <class A, int R, int NT, class Sched, bool Contig>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, R >= 16 ? 2 : 1)
     wide_kernel(__grid_constant__ const LiftParams p) {
   using V = typename A::V;
   using W = typename A::Store;
@@ -1201,6 +1201,160 @@ __global__ void __launch_bounds__(NT)
 
 template <class A, int R, int NT> constexpr size_t wide_smem_bytes() {
   return size_t(WideStages<A>::value) * R * NT * sizeof(typename A::Store);
+}
+
+// Tile kernel: periodic pencils of 128 to 512 points along a strided axis.
+// A tile is NT / G column groups of kCols columns (G = n / R chunks per
+// pencil) times the n pencil rows; it is copied between HBM and shared
+// memory in row order with 16-byte cp.async and stores (lanes along the
+// row, coalesced), in a row-major layout where each chunk's R rows are
+// followed by PAD bytes. Each thread then holds the same chunk of kCols
+// adjacent pencils as rows of A::V in registers, as in the wide kernel (the
+// G chunks of a column group are lanes 32 / G apart and exchange by
+// shuffle), and writes its rows back before the tile is stored. PAD makes
+// the chunk blocks' bank offsets step by one warp-row segment (32 / G
+// groups of kCols columns), so the rows a warp reads at once fall on
+// distinct banks.
+//
+// Tiles are software pipelined over TileStages buffers: the tile TileStages
+// - 1 ahead is in flight while the current one is transformed.
+template <class A> struct TileStages {
+  static constexpr int value = sizeof(typename A::Store) == 16 ? 2 : 3;
+};
+// Bytes of one tile buffer: n * row bytes = R * NT row vectors, plus the
+// padding of G chunks (PAD <= one warp-row segment of 32 / G row vectors).
+template <class A, int R, int NT> struct TileStageBytes {
+  static constexpr int value =
+      (R * NT + 32) * static_cast<int>(sizeof(typename A::Store));
+};
+template <class A, int R, int NT> constexpr size_t tile_smem_bytes() {
+  return size_t(TileStages<A>::value) * TileStageBytes<A, R, NT>::value;
+}
+
+// Geometry of one tile of a job.
+struct TileGeo {
+  long long gc0;     // first column of the tile
+  long long columns;
+  int log2G;         // chunks per pencil
+  int log2rb;        // bytes per tile row
+  int pad;           // bytes after each chunk's rows
+  int cpitch;        // bytes per chunk block: R rows + pad
+};
+
+template <class A, int LOG2R, int LOG2NT>
+__device__ __forceinline__ TileGeo tile_geo(LiftJob const &job,
+                                            long long tile) {
+  constexpr int LOG2CW = Log2<A::kCols>::value;
+  constexpr int LOG2W = Log2<sizeof(typename A::Store)>::value;
+  TileGeo g;
+  g.log2G = job.log2_n - LOG2R;
+  int const log2tcg = LOG2NT - g.log2G;  // column groups per tile
+  g.gc0 = (tile - job.tile_begin) << (log2tcg + LOG2CW);
+  g.columns = job.columns;
+  g.log2rb = log2tcg + LOG2W;
+  g.pad = (1 << (5 - g.log2G + LOG2W)) & 127;  // one warp-row segment
+  g.cpitch = (1 << (LOG2R + g.log2rb)) + g.pad;
+  return g;
+}
+
+template <class A, int R, int NT, class Sched>
+__global__ void __launch_bounds__(NT, 2)
+    tile_kernel(__grid_constant__ const LiftParams p) {
+  using V = typename A::V;
+  using W = typename A::Store;
+  using E = typename A::Elem;
+  constexpr int CW = A::kCols;
+  constexpr int LOG2R = Log2<R>::value;
+  constexpr int LOG2NT = Log2<NT>::value;
+  constexpr int S = TileStages<A>::value;
+  constexpr int PER = 16 / sizeof(E);  // columns per 16-byte piece
+  constexpr int LOG2PER = Log2<PER>::value;
+  constexpr int STAGE = TileStageBytes<A, R, NT>::value;
+  static_assert(sizeof(W) == CW * sizeof(E), "row vector size");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+
+  int const t = threadIdx.x;
+  int const lane = t & 31;
+  long long const T = p.total_tiles;
+  long long const u0 = T * blockIdx.x / gridDim.x;
+  long long const u1 = T * (blockIdx.x + 1) / gridDim.x;
+  if (u0 >= u1) return;
+  bool const many = p.jobs != nullptr;
+  int jl = many ? find_job(p, u0) : 0;
+  int jc = jl;
+  auto job_of = [&](int &ji, long long tile) -> LiftJob const & {
+    if (!many) return p.job;
+    while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
+    return p.jobs[ji];
+  };
+  // Element offset of tile column `tc` (a multiple of PER) in row k; columns
+  // past the job's last one read the last PER columns instead.
+  auto elem = [](LiftJob const &job, TileGeo const &g, long long tc,
+                 int k) {
+    long long gc = g.gc0 + tc;
+    if (gc > g.columns - PER) gc = g.columns - PER;
+    int const log2B = job.log2_inner;
+    return ((gc >> log2B) << job.log2_astride) +
+           (gc & ((1LL << log2B) - 1)) +
+           (static_cast<long long>(k) << job.log2_kstride);
+  };
+  auto smem_off = [](TileGeo const &g, int k, int q) {
+    return (k >> LOG2R) * g.cpitch + ((k & (R - 1)) << g.log2rb) + q * 16;
+  };
+  auto prefetch = [&](long long tile) {
+    LiftJob const &job = job_of(jl, tile);
+    TileGeo const g = tile_geo<A, LOG2R, LOG2NT>(job, tile);
+    unsigned char *const st = smem_raw + static_cast<int>(tile % S) * STAGE;
+    E const *const src = reinterpret_cast<E const *>(job.base);
+    int const log2q = g.log2rb - 4;  // pieces per row
+    int const pieces = 1 << (job.log2_n + log2q);
+    for (int i = t; i < pieces; i += NT) {
+      int const k = i >> log2q;
+      int const q = i & ((1 << log2q) - 1);
+      cp_async<16>(st + smem_off(g, k, q), src + elem(job, g, q << LOG2PER, k));
+    }
+    cp_async_commit();
+  };
+
+#pragma unroll
+  for (int k = 0; k < S - 1; ++k)
+    if (u0 + k < u1) prefetch(u0 + k); else cp_async_commit();
+  for (long long u = u0; u < u1; ++u) {
+    __syncthreads();  // the buffer the next prefetch fills is free
+    if (u + S - 1 < u1) prefetch(u + S - 1); else cp_async_commit();
+    cp_async_wait_group<S - 1>();
+    __syncthreads();  // every thread's copies of tile u are visible
+    LiftJob const &job = job_of(jc, u);
+    TileGeo const g = tile_geo<A, LOG2R, LOG2NT>(job, u);
+    unsigned char *const st = smem_raw + static_cast<int>(u % S) * STAGE;
+    int const log2gw = 5 - g.log2G;  // column groups per warp row
+    int const c = lane >> log2gw;
+    int const grp = ((t >> 5) << log2gw) | (lane & ((1 << log2gw) - 1));
+    unsigned char *const mine =
+        st + c * g.cpitch + grp * static_cast<int>(sizeof(W));
+    V v[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+      v[j] = A::load(*reinterpret_cast<W const *>(mine + (j << g.log2rb)));
+    RoundCtx<A, NT> ctx(t, c, 1 << g.log2G, g.log2G, lane, 1, nullptr,
+                        nullptr, log2gw);
+    Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+      *reinterpret_cast<W *>(mine + (j << g.log2rb)) = A::store(v[j]);
+    __syncthreads();  // the transformed tile is in shared memory
+    E *const dst = reinterpret_cast<E *>(job.dst_base);
+    int const log2q = g.log2rb - 4;
+    int const pieces = 1 << (job.log2_n + log2q);
+    for (int i = t; i < pieces; i += NT) {
+      int const k = i >> log2q;
+      int const q = i & ((1 << log2q) - 1);
+      if (g.gc0 + (q << LOG2PER) < g.columns)
+        *reinterpret_cast<uint4 *>(dst + elem(job, g, q << LOG2PER, k)) =
+            *reinterpret_cast<uint4 const *>(st + smem_off(g, k, q));
+    }
+  }
+  cp_async_wait_all();
 }
 
 // Dynamic shared memory of one CTA (an upper bound over every column shape:

@@ -53,6 +53,7 @@ struct AxisView {
   // FP32 and FP64 run faster there on the direct kernel, which needs fewer
   // registers per pencil).
   bool wide_last = false;
+  int log2_es = 0;  // log2 of the element size in bytes
 };
 
 AxisView axis_view(unsigned long long base, int ndim, int64_t const *level,
@@ -60,9 +61,11 @@ AxisView axis_view(unsigned long long base, int ndim, int64_t const *level,
 
 // Stage::R names the kernel and its chunk size: R > 0 the staged kernel with
 // chunks of R points, -R the direct kernel, kWide + R the wide kernel on a
-// strided axis, kWideContig + R the wide kernel on the last axis.
+// strided axis, kWideContig + R the wide kernel on the last axis, kTile + R
+// the tile kernel.
 constexpr int kWide = 64;
 constexpr int kWideContig = 128;
+constexpr int kTile = 192;
 
 // One stage of an axis transform: a job for one kernel. The stages of one
 // axis must run in order; stages of different grids are independent.

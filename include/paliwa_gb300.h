@@ -167,8 +167,9 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
  * it stores) and kernel: R > 0 the staged kernel with chunks of R points,
  * -R the direct kernel (pencils in registers), 64 + R and 128 + R the wide
  * kernel (rows of adjacent columns in registers) on a strided axis and on
- * the last axis, 192 + R the tile kernel (row-major tiles in shared memory,
- * rows of adjacent columns in registers); `kernels` may be null. Call with
+ * the last axis, 192 + R and 256 + R the tile kernel (row-major tiles in
+ * shared memory, rows of adjacent columns in registers) for pencils of up to
+ * 32 chunks and longer ones; `kernels` may be null. Call with
  * capacity 0 to get *nlaunches first. */
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,

@@ -61,6 +61,17 @@ int chunk_for(int log2_n) {
 // pieces; 32 lanes: 8): measured on a 2^26-point FP32 grid, the first axis
 // at n = 256 fell from 2.2 TB/s (G = 16) to 0.47 TB/s (G = 32), so longer
 // pencils go to the staged kernel.
+// log2 of the bytes of one copied piece of the tile kernel (lift.cuh,
+// tile_geo) for 256 threads: 8 when the chunk padding (one warp-row segment)
+// or the tile row is not a multiple of 16 bytes, else 16.
+int tile_piece_log2(int log2G, int log2_row_bytes) {
+  static_assert(kThreads == 256, "tile geometry assumes 256 threads");
+  int const log2seg = log2G >= 5 ? log2_row_bytes : 5 - log2G + log2_row_bytes;
+  int const pad = (1 << log2seg) & 127;
+  int const log2rb = 8 - log2G + log2_row_bytes;
+  return (pad & 15) != 0 || log2rb < 4 ? 3 : 4;
+}
+
 int wide_chunk(int log2_n) {
   if (log2_n <= 4) return 1 << log2_n;
   if (log2_n <= 6) return 1 << (log2_n - 2);
@@ -193,15 +204,20 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
     bool const wide_last = canon && last && v.wide_last && log2G <= 5 &&
                            v.columns >= (1LL << v.log2_row);
     bool const direct = R == (1 << v.log2_n) || (last && log2G <= 5);
-    // Strided pencils of 128 to 512 points (256 with 8-byte row vectors,
-    // whose chunk padding would break 16-byte alignment at G = 32) whose
-    // inner extent holds whole 16-byte pieces run on the tile kernel.
-    int const log2_row_bytes = v.log2_row + v.log2_es;
+    // Strided pencils of 128 points and more whose inner extent holds whole
+    // copy pieces run on the tile kernel, up to the length where it was
+    // measured faster than the staged kernel (first axis of 2^26-point
+    // grids, and the 4D CT batch): 4096 points in FP32 (2.8 against 1.8
+    // TB/s at 1024), 512 in FP64, 256 in FP32c (at G = 32 its 8-byte row
+    // vectors need 8-byte copy pieces, and beyond 32 chunks the batch ran
+    // slower than on the staged kernel).
+    int const tile_log2G_max = v.wide_last ? 4 : v.log2_es == 3 ? 5 : 8;
     bool const tile = canon && !last && R == 16 && log2G >= 3 &&
-                      log2G <= (log2_row_bytes == 4 ? 5 : 4) &&
-                      v.log2_inner + v.log2_es >= 4;
+                      log2G <= tile_log2G_max &&
+                      v.log2_inner + v.log2_es >=
+                          tile_piece_log2(log2G, v.log2_row + v.log2_es);
     if (tile) {
-      st.R = kTile + 16;
+      st.R = (log2G <= 5 ? kTile : kTileLong) + 16;
       st.job.col_tiles =
           ceil_div(v.columns >> v.log2_row, kThreads >> log2G);
     } else if (wide) {

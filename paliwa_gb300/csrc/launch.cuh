@@ -55,12 +55,13 @@ void launch_wide_r(LiftParams const &p, cudaStream_t s) {
                     wide_smem_bytes<A, R, kThreads>(), p, s, per_sm, sms);
 }
 
-template <class A, int R, class Sched>
+template <class A, int R, class Sched, bool Long>
 void launch_tile_r(LiftParams const &p, cudaStream_t s) {
   static thread_local int per_sm = 0;
   static thread_local int sms = 0;
-  launch_persistent(tile_kernel<A, R, kThreads, Sched>,
-                    tile_smem_bytes<A, R, kThreads>(), p, s, per_sm, sms);
+  launch_persistent(tile_kernel<A, R, kThreads, Sched, Long>,
+                    tile_smem_bytes<A, R, kThreads, Long>(), p, s, per_sm,
+                    sms);
 }
 
 // Row policy A (arith.cuh), code kWide + R (strided axis) or kWideContig + R
@@ -79,7 +80,8 @@ void launch_wide(int sched, int code, LiftParams const &p, cudaStream_t s) {
     case kWideContig + 4: return launch_wide_r<A, 4, Sched, true>(p, s);
     case kWideContig + 8: return launch_wide_r<A, 8, Sched, true>(p, s);
     case kWideContig + 16: return launch_wide_r<A, 16, Sched, true>(p, s);
-    case kTile + 16: return launch_tile_r<A, 16, Sched>(p, s);
+    case kTile + 16: return launch_tile_r<A, 16, Sched, false>(p, s);
+    case kTileLong + 16: return launch_tile_r<A, 16, Sched, true>(p, s);
     }
     throw StatusError(2, "bad chunk size");
   };

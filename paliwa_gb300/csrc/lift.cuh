@@ -1051,8 +1051,11 @@ template <class A, int R> struct ContigPieces {
   }
 };
 
+// Register budgets: 2, 3 and 4 CTAs of 256 threads per SM for R = 16, 8
+// and <= 4 (128, 80 and 64 registers); one register above a budget costs a
+// whole CTA per SM, measured as 10% of the R = 8 kernel's throughput.
 template <class A, int R, int NT, class Sched, bool Contig>
-__global__ void __launch_bounds__(NT, R >= 16 ? 2 : 1)
+__global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
     wide_kernel(__grid_constant__ const LiftParams p) {
   using V = typename A::V;
   using W = typename A::Store;
@@ -1203,32 +1206,53 @@ template <class A, int R, int NT> constexpr size_t wide_smem_bytes() {
   return size_t(WideStages<A>::value) * R * NT * sizeof(typename A::Store);
 }
 
-// Tile kernel: periodic pencils of 128 to 512 points along a strided axis.
+// Tile kernel: periodic pencils of 128 to 4096 points along a strided axis.
 // A tile is NT / G column groups of kCols columns (G = n / R chunks per
 // pencil) times the n pencil rows; it is copied between HBM and shared
-// memory in row order with 16-byte cp.async and stores (lanes along the
-// row, coalesced), in a row-major layout where each chunk's R rows are
+// memory in row order with 16- or 8-byte cp.async and stores (lanes along
+// the row, coalesced), in a row-major layout where each chunk's R rows are
 // followed by PAD bytes. Each thread then holds the same chunk of kCols
-// adjacent pencils as rows of A::V in registers, as in the wide kernel (the
-// G chunks of a column group are lanes 32 / G apart and exchange by
-// shuffle), and writes its rows back before the tile is stored. PAD makes
-// the chunk blocks' bank offsets step by one warp-row segment (32 / G
-// groups of kCols columns), so the rows a warp reads at once fall on
-// distinct banks.
+// adjacent pencils as rows of A::V in registers, as in the wide kernel, and
+// writes its rows back before the tile is stored.
 //
-// Tiles are software pipelined over TileStages buffers: the tile TileStages
-// - 1 ahead is in flight while the current one is transformed.
-template <class A> struct TileStages {
-  static constexpr int value = sizeof(typename A::Store) == 16 ? 2 : 3;
+// Lanes: for G <= 32 the G chunks of a column group are lanes 32 / G apart
+// (a warp holds 32 / G column groups) and exchange by shuffle; for G > 32 a
+// warp holds 32 consecutive chunks of one column group and the exchanges go
+// through shared memory (one barrier per level pass). PAD is one warp-row
+// segment (the bytes of the column groups a warp holds, at least one row
+// vector): it steps the chunk blocks' bank offsets so that the rows a warp
+// reads at once fall on distinct banks. Pieces are 8 bytes when PAD is not
+// a multiple of 16 (8-byte row vectors with 32 or more chunks).
+//
+// Two forms (Long): pencils of up to 32 chunks (shuffles only) and longer
+// ones (G > 32). The short form gives each CTA a contiguous range of tiles
+// and keeps three tile buffers in flight for 8-byte row vectors (two for
+// 16-byte ones); measured on the 4D CT batch this is faster for short
+// pencils. The long form double buffers and has the CTAs take every
+// gridDim.x-th tile, so that the CTAs running at one time work on
+// neighbouring tiles: its tile rows are 8 to 64 bytes, and neighbouring
+// tiles share DRAM sectors and pages (FP32, 4096-point pencils: 1.6 against
+// 1.1 TB/s with contiguous ranges).
+template <class A, bool Long> struct TileStages {
+  static constexpr int value =
+      Long || sizeof(typename A::Store) == 16 ? 2 : 3;
 };
 // Bytes of one tile buffer: n * row bytes = R * NT row vectors, plus the
-// padding of G chunks (PAD <= one warp-row segment of 32 / G row vectors).
-template <class A, int R, int NT> struct TileStageBytes {
-  static constexpr int value =
-      (R * NT + 32) * static_cast<int>(sizeof(typename A::Store));
+// padding of G chunks (at most max(32, G) row vectors).
+template <class A, int R, int NT, bool Long> struct TileStageBytes {
+  static constexpr int value = (R * NT + (Long ? 256 : 32)) *
+                               static_cast<int>(sizeof(typename A::Store));
 };
-template <class A, int R, int NT> constexpr size_t tile_smem_bytes() {
-  return size_t(TileStages<A>::value) * TileStageBytes<A, R, NT>::value;
+// Chunk heads and the two exchange buffers of RoundCtx (G > 32).
+template <class A, int NT, bool Long> struct TileXchBytes {
+  static constexpr int value =
+      Long ? 3 * NT * static_cast<int>(sizeof(typename A::V)) : 0;
+};
+template <class A, int R, int NT, bool Long>
+constexpr size_t tile_smem_bytes() {
+  return size_t(TileStages<A, Long>::value) *
+             TileStageBytes<A, R, NT, Long>::value +
+         TileXchBytes<A, NT, Long>::value;
 }
 
 // Geometry of one tile of a job.
@@ -1237,6 +1261,7 @@ struct TileGeo {
   long long columns;
   int log2G;         // chunks per pencil
   int log2rb;        // bytes per tile row
+  int log2pb;        // bytes per copied piece (3 or 4)
   int pad;           // bytes after each chunk's rows
   int cpitch;        // bytes per chunk block: R rows + pad
 };
@@ -1252,12 +1277,14 @@ __device__ __forceinline__ TileGeo tile_geo(LiftJob const &job,
   g.gc0 = (tile - job.tile_begin) << (log2tcg + LOG2CW);
   g.columns = job.columns;
   g.log2rb = log2tcg + LOG2W;
-  g.pad = (1 << (5 - g.log2G + LOG2W)) & 127;  // one warp-row segment
+  int const log2seg = g.log2G >= 5 ? LOG2W : 5 - g.log2G + LOG2W;
+  g.pad = (1 << log2seg) & 127;  // one warp-row segment
   g.cpitch = (1 << (LOG2R + g.log2rb)) + g.pad;
+  g.log2pb = (g.pad & 15) != 0 || g.log2rb < 4 ? 3 : 4;
   return g;
 }
 
-template <class A, int R, int NT, class Sched>
+template <class A, int R, int NT, class Sched, bool Long>
 __global__ void __launch_bounds__(NT, 2)
     tile_kernel(__grid_constant__ const LiftParams p) {
   using V = typename A::V;
@@ -1266,92 +1293,135 @@ __global__ void __launch_bounds__(NT, 2)
   constexpr int CW = A::kCols;
   constexpr int LOG2R = Log2<R>::value;
   constexpr int LOG2NT = Log2<NT>::value;
-  constexpr int S = TileStages<A>::value;
-  constexpr int PER = 16 / sizeof(E);  // columns per 16-byte piece
-  constexpr int LOG2PER = Log2<PER>::value;
-  constexpr int STAGE = TileStageBytes<A, R, NT>::value;
+  constexpr int S = TileStages<A, Long>::value;
+  constexpr int LOG2ES = Log2<sizeof(E)>::value;
+  constexpr int STAGE = TileStageBytes<A, R, NT, Long>::value;
   static_assert(sizeof(W) == CW * sizeof(E), "row vector size");
+  static_assert(sizeof(W) >= 8, "pieces of at least 8 bytes");
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *const heads =
+      Long ? reinterpret_cast<V *>(smem_raw + S * STAGE) : nullptr;
+  V *const xch = Long ? heads + NT : nullptr;
 
   int const t = threadIdx.x;
   int const lane = t & 31;
   long long const T = p.total_tiles;
-  long long const u0 = T * blockIdx.x / gridDim.x;
-  long long const u1 = T * (blockIdx.x + 1) / gridDim.x;
-  if (u0 >= u1) return;
+  // Tiles of this CTA: u0, u0 + step, ... below u1.
+  long long const step = Long ? gridDim.x : 1;
+  long long const u0 = Long ? blockIdx.x : T * blockIdx.x / gridDim.x;
+  long long const u1 = Long ? T : T * (blockIdx.x + 1) / gridDim.x;
   bool const many = p.jobs != nullptr;
-  int jl = many ? find_job(p, u0) : 0;
-  int jc = jl;
+  int jl = 0, jc = 0;
+  // Job of `tile` (tiles only increase along each cursor): the current job,
+  // the next one, or a binary search over the rest.
   auto job_of = [&](int &ji, long long tile) -> LiftJob const & {
     if (!many) return p.job;
-    while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
+    if (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) {
+      ++ji;
+      if (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) {
+        int lo = ji + 1, hi = p.njobs - 1;
+        while (lo < hi) {
+          int const mid = (lo + hi + 1) >> 1;
+          if (p.jobs[mid].tile_begin <= tile)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        ji = lo;
+      }
+    }
     return p.jobs[ji];
   };
-  // Element offset of tile column `tc` (a multiple of PER) in row k; columns
-  // past the job's last one read the last PER columns instead.
-  auto elem = [](LiftJob const &job, TileGeo const &g, long long tc,
-                 int k) {
+  // Element offset of tile column `tc` (a multiple of the piece's columns)
+  // in row k; pieces past the job's last column read its last piece.
+  auto elem = [](LiftJob const &job, TileGeo const &g, long long tc, int k) {
+    long long const last = g.columns - (1 << (g.log2pb - LOG2ES));
     long long gc = g.gc0 + tc;
-    if (gc > g.columns - PER) gc = g.columns - PER;
+    if (gc > last) gc = last;
     int const log2B = job.log2_inner;
     return ((gc >> log2B) << job.log2_astride) +
            (gc & ((1LL << log2B) - 1)) +
            (static_cast<long long>(k) << job.log2_kstride);
   };
   auto smem_off = [](TileGeo const &g, int k, int q) {
-    return (k >> LOG2R) * g.cpitch + ((k & (R - 1)) << g.log2rb) + q * 16;
+    return (k >> LOG2R) * g.cpitch + ((k & (R - 1)) << g.log2rb) +
+           (q << g.log2pb);
   };
-  auto prefetch = [&](long long tile) {
+  auto prefetch = [&](long long tile, int buf) {
     LiftJob const &job = job_of(jl, tile);
     TileGeo const g = tile_geo<A, LOG2R, LOG2NT>(job, tile);
-    unsigned char *const st = smem_raw + static_cast<int>(tile % S) * STAGE;
+    unsigned char *const st = smem_raw + buf * STAGE;
     E const *const src = reinterpret_cast<E const *>(job.base);
-    int const log2q = g.log2rb - 4;  // pieces per row
+    int const log2q = g.log2rb - g.log2pb;  // pieces per row
     int const pieces = 1 << (job.log2_n + log2q);
+    int const cols_q = g.log2pb - LOG2ES;   // log2 columns per piece
     for (int i = t; i < pieces; i += NT) {
       int const k = i >> log2q;
       int const q = i & ((1 << log2q) - 1);
-      cp_async<16>(st + smem_off(g, k, q), src + elem(job, g, q << LOG2PER, k));
+      E const *const from = src + elem(job, g, static_cast<long long>(q)
+                                                    << cols_q, k);
+      if (g.log2pb == 4)
+        cp_async<16>(st + smem_off(g, k, q), from);
+      else
+        cp_async<8>(st + smem_off(g, k, q), from);
     }
     cp_async_commit();
   };
 
+  // The CTA's k-th tile (u0 + k * step) uses buffer k % S.
 #pragma unroll
   for (int k = 0; k < S - 1; ++k)
-    if (u0 + k < u1) prefetch(u0 + k); else cp_async_commit();
-  for (long long u = u0; u < u1; ++u) {
+    if (u0 + k * step < u1) prefetch(u0 + k * step, k); else cp_async_commit();
+  int slot = 0;  // buffer of tile u
+  for (long long u = u0; u < u1;
+       u += step, slot = slot + 1 == S ? 0 : slot + 1) {
     __syncthreads();  // the buffer the next prefetch fills is free
-    if (u + S - 1 < u1) prefetch(u + S - 1); else cp_async_commit();
+    long long const ahead = u + (S - 1) * step;
+    int const ahead_slot = (slot + S - 1) % S;
+    if (ahead < u1) prefetch(ahead, ahead_slot); else cp_async_commit();
     cp_async_wait_group<S - 1>();
     __syncthreads();  // every thread's copies of tile u are visible
     LiftJob const &job = job_of(jc, u);
     TileGeo const g = tile_geo<A, LOG2R, LOG2NT>(job, u);
-    unsigned char *const st = smem_raw + static_cast<int>(u % S) * STAGE;
-    int const log2gw = 5 - g.log2G;  // column groups per warp row
-    int const c = lane >> log2gw;
-    int const grp = ((t >> 5) << log2gw) | (lane & ((1 << log2gw) - 1));
+    unsigned char *const st = smem_raw + slot * STAGE;
+    int c, grp, log2ls;
+    if (!Long || g.log2G <= 5) {  // chunks of a column group 32 / G lanes apart
+      log2ls = 5 - g.log2G;
+      c = lane >> log2ls;
+      grp = ((t >> 5) << log2ls) | (lane & ((1 << log2ls) - 1));
+    } else {             // 32 consecutive chunks per warp
+      log2ls = 0;
+      c = t & ((1 << g.log2G) - 1);
+      grp = t >> g.log2G;
+    }
     unsigned char *const mine =
         st + c * g.cpitch + grp * static_cast<int>(sizeof(W));
     V v[R];
 #pragma unroll
     for (int j = 0; j < R; ++j)
       v[j] = A::load(*reinterpret_cast<W const *>(mine + (j << g.log2rb)));
-    RoundCtx<A, NT> ctx(t, c, 1 << g.log2G, g.log2G, lane, 1, nullptr,
-                        nullptr, log2gw);
+    RoundCtx<A, NT> ctx(t, c, 1 << g.log2G, g.log2G, lane, 1, heads, xch,
+                        log2ls);
     Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
 #pragma unroll
     for (int j = 0; j < R; ++j)
       *reinterpret_cast<W *>(mine + (j << g.log2rb)) = A::store(v[j]);
     __syncthreads();  // the transformed tile is in shared memory
     E *const dst = reinterpret_cast<E *>(job.dst_base);
-    int const log2q = g.log2rb - 4;
+    int const log2q = g.log2rb - g.log2pb;
     int const pieces = 1 << (job.log2_n + log2q);
+    int const cols_q = g.log2pb - LOG2ES;
     for (int i = t; i < pieces; i += NT) {
       int const k = i >> log2q;
       int const q = i & ((1 << log2q) - 1);
-      if (g.gc0 + (q << LOG2PER) < g.columns)
-        *reinterpret_cast<uint4 *>(dst + elem(job, g, q << LOG2PER, k)) =
-            *reinterpret_cast<uint4 const *>(st + smem_off(g, k, q));
+      long long const tc = static_cast<long long>(q) << cols_q;
+      if (g.gc0 + tc >= g.columns) continue;
+      unsigned char const *const from = st + smem_off(g, k, q);
+      E *const to = dst + elem(job, g, tc, k);
+      if (g.log2pb == 4)
+        *reinterpret_cast<uint4 *>(to) = *reinterpret_cast<uint4 const *>(from);
+      else
+        *reinterpret_cast<uint2 *>(to) = *reinterpret_cast<uint2 const *>(from);
     }
   }
   cp_async_wait_all();

@@ -62,10 +62,12 @@ AxisView axis_view(unsigned long long base, int ndim, int64_t const *level,
 // Stage::R names the kernel and its chunk size: R > 0 the staged kernel with
 // chunks of R points, -R the direct kernel, kWide + R the wide kernel on a
 // strided axis, kWideContig + R the wide kernel on the last axis, kTile + R
-// the tile kernel.
+// and kTileLong + R the tile kernel for pencils of up to 32 chunks and
+// longer ones.
 constexpr int kWide = 64;
 constexpr int kWideContig = 128;
 constexpr int kTile = 192;
+constexpr int kTileLong = 256;
 
 // One stage of an axis transform: a job for one kernel. The stages of one
 // axis must run in order; stages of different grids are independent.

@@ -130,6 +130,38 @@ def test_wide_edges_bit_exact(level, lmin, wavelet):
             assert np.array_equal(got, want), (level, dt, wavelet, forward)
 
 
+# Strided pencils of 128 to 4096 points on the tile kernel: chunks exchanged
+# by shuffle (G <= 32) and through shared memory (G > 32), 8- and 16-byte
+# copy pieces, inner extents narrower than a tile row, partial tiles.
+TILE_SHAPES = [((7, 3), (0, 0)), ((8, 2), (1, 0)), ((9, 4), (0, 1)),
+               ((10, 2), (0, 1)), ((11, 3), (2, 0)), ((12, 2), (0, 0)),
+               ((2, 10, 3), (0, 1, 0)), ((8, 1, 2), (0, 0, 0)),
+               ((9, 6), (3, 0))]
+
+
+@pytest.mark.parametrize("wavelet", WAVELETS)
+@pytest.mark.parametrize("level,lmin", TILE_SHAPES)
+def test_tile_shapes_exact(level, lmin, wavelet):
+    """FP64 and FP32 bit-identical to the oracle, FP32c bit-identical to
+    the compensated model, forward and inverse."""
+    from compensated import hierarchize as model
+    O = import_oracle()
+    for dt in (np.float64, np.float32):
+        x = random_input(level, 23).astype(dt)
+        for forward in (True, False):
+            want = O.hierarchize(x.copy(), level, lmin, tuple(level), wavelet,
+                                 forward=forward)
+            got = gpu_transform(x, level, lmin, tuple(level), wavelet,
+                                forward)
+            assert np.array_equal(got, want), (level, dt, wavelet, forward)
+    x = random_input(level, 29).astype(np.float32)
+    for forward in (True, False):
+        want = model(x, level, lmin, wavelet, forward)
+        got = gpu_transform(x, level, lmin, tuple(level), wavelet, forward,
+                            compensated=True)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
 LONG = [((14,), (0,)), ((15,), (2,)), ((17,), (0,)), ((16, 1), (3, 0)),
         ((2, 15), (0, 0)), ((14, 2), (0, 1)), ((1, 1, 1, 17), (1, 1, 1, 1))]
 

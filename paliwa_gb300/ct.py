@@ -170,6 +170,109 @@ class Batch:
             pass
 
 
+def group_ranges(sizes, groups):
+    """Split consecutive items of the given sizes into at most ``groups``
+    consecutive, non-empty ranges [a, b) of about equal total size."""
+    total = sum(sizes)
+    groups = max(1, min(int(groups), len(sizes)))
+    out, a, acc = [], 0, 0
+    for i, s in enumerate(sizes):
+        acc += s
+        left = len(sizes) - (i + 1)
+        want = len(out) + 1
+        if want < groups and (acc * groups >= total * want
+                              or left == groups - want):
+            out.append((a, i + 1))
+            a = i + 1
+    out.append((a, len(sizes)))
+    return out
+
+
+class HostBatch:
+    """Transforms of a batch of grids held in host memory, with the copies
+    to and from the device overlapped with the transforms.
+
+    The grids are packed into one device buffer (the layout of
+    :func:`packed_grids`, which is also the layout of the host buffers) and
+    split into ``groups`` consecutive groups of about equal size, each with
+    its own plan (:class:`Batch`). :meth:`run` copies group g in on one copy
+    stream, transforms it on the compute stream once it has landed, and
+    copies it out on a second copy stream once transformed, so that group
+    g + 1 arrives and group g - 1 leaves while group g is transformed. Host
+    buffers should be pinned (``pin_memory()``) for the copies to be
+    asynchronous."""
+
+    def __init__(self, levels, minimum_level, maximum_level,
+                 wavelet_name="hat", dtype=None, compensated=False, groups=8,
+                 device=None, align=64):
+        import torch
+        dtype = torch.float32 if dtype is None else dtype
+        self.levels = [tuple(int(x) for x in l) for l in levels]
+        self.buf, self.grids = packed_grids(self.levels, dtype,
+                                            device or "cuda", align)
+        base = self.buf.data_ptr()
+        esz = self.buf.element_size()
+        starts = [(g.data_ptr() - base) // esz for g in self.grids]
+        ends = starts[1:] + [self.buf.numel()]
+        self.ranges = group_ranges([e - s for s, e in zip(starts, ends)],
+                                   groups)
+        self.spans = [(starts[a], ends[b - 1]) for a, b in self.ranges]
+        self.batches = [Batch(self.grids[a:b], self.levels[a:b],
+                              minimum_level, maximum_level, wavelet_name,
+                              compensated) for a, b in self.ranges]
+        dev = self.buf.device
+        self._streams = [torch.cuda.Stream(dev) for _ in range(3)]
+        self.points = sum(g.numel() for g in self.grids)
+
+    def numel(self):
+        """Elements of the packed host (and device) buffers."""
+        return self.buf.numel()
+
+    def run(self, host_in, host_out, steps=("hierarchize", "dehierarchize"),
+            stream=None):
+        """Copy ``host_in`` in, apply the ``steps`` (method names of
+        :class:`Batch`, in order) to every grid, copy the result to
+        ``host_out``. Ordered after the current (or given) stream, which
+        waits for the last copy out."""
+        import torch
+        if host_in.numel() != self.buf.numel() or \
+                host_out.numel() != self.buf.numel():
+            raise _lib.InvalidArgument("host buffers must hold numel() "
+                                       "elements in the packed layout")
+        cur = stream or torch.cuda.current_stream(self.buf.device)
+        s_in, s_run, s_out = self._streams
+        start = torch.cuda.Event()
+        start.record(cur)
+        for s in self._streams:
+            s.wait_event(start)
+        landed, done = [], []
+        with torch.cuda.stream(s_in):
+            for a, b in self.spans:
+                self.buf[a:b].copy_(host_in[a:b], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(s_in)
+                landed.append(ev)
+        for bt, ev in zip(self.batches, landed):
+            s_run.wait_event(ev)
+            for name in steps:
+                getattr(bt, name)(s_run)
+            ev2 = torch.cuda.Event()
+            ev2.record(s_run)
+            done.append(ev2)
+        with torch.cuda.stream(s_out):
+            for (a, b), ev in zip(self.spans, done):
+                s_out.wait_event(ev)
+                host_out[a:b].copy_(self.buf[a:b], non_blocking=True)
+        end = torch.cuda.Event()
+        end.record(s_out)
+        cur.wait_event(end)
+
+    def close(self):
+        for bt in self.batches:
+            bt.close()
+        self.batches = []
+
+
 class CombinationTechnique:
     """Sparse-grid combine / restrict / scatter of a combination scheme."""
 

@@ -265,3 +265,31 @@ def test_batch_compensated_bit_exact_model():
             assert np.array_equal(got.view(np.uint32),
                                   want.view(np.uint32)), (lv, forward)
     b.close()
+
+
+def test_host_batch_matches_device_batch():
+    """HostBatch (grids in pinned host memory, copies overlapped with the
+    transforms of other groups) gives the device Batch's bits."""
+    import torch
+    levels, _ = pct.combination_scheme(4, 13, 3, 1)
+    lmin, lmax = (1, 1, 1, 1), (10, 10, 10, 10)
+    hb = pct.HostBatch(levels, lmin, lmax, "biorthogonal", torch.float32,
+                       compensated=True, groups=5)
+    assert len(hb.batches) == 5
+    rng = np.random.default_rng(13)
+    host_in = torch.from_numpy(
+        rng.uniform(-1, 1, hb.numel()).astype(np.float32)).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    for steps in (("hierarchize",), ("hierarchize", "dehierarchize")):
+        hb.run(host_in, host_out, steps)
+        torch.cuda.synchronize()
+        buf, gs = pct.packed_grids(levels, torch.float32)
+        buf.copy_(host_in)
+        b = pct.Batch(gs, levels, lmin, lmax, "biorthogonal",
+                      compensated=True)
+        for name in steps:
+            getattr(b, name)()
+        torch.cuda.synchronize()
+        assert torch.equal(buf.cpu(), host_out), steps
+        b.close()
+    hb.close()

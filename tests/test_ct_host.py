@@ -23,3 +23,17 @@ def test_classical_scheme_counts_6d():
 def test_subspace_count_matches_oracle(oracle_mod):
     levels, _ = pct.combination_scheme(3, 9, 2, 1)
     assert pct.subspace_count(levels) == oracle_mod.subspace_counts(levels)
+
+
+def test_group_ranges_cover_in_order():
+    from paliwa_gb300.ct import group_ranges
+    for sizes, groups in (([5, 1, 1, 1, 8, 2, 2], 3), ([1] * 10, 4),
+                          ([3], 8), ([1, 1], 5), ([7, 7, 7, 7], 2),
+                          (list(range(1, 40)), 8)):
+        r = group_ranges(sizes, groups)
+        assert r[0][0] == 0 and r[-1][1] == len(sizes)
+        assert all(a < b for a, b in r)
+        assert all(r[i][1] == r[i + 1][0] for i in range(len(r) - 1))
+        assert len(r) <= max(1, min(groups, len(sizes)))
+    r = group_ranges([1] * 64, 8)
+    assert [b - a for a, b in r] == [8] * 8

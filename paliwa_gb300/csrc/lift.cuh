@@ -1003,6 +1003,65 @@ __device__ __forceinline__ int find_job(LiftParams const &p, long long tile) {
   return lo;
 }
 
+// A forward-only cursor over a launch's job list, used by all lanes of a
+// warp with the same tile. The cursor lives in a warp-private shared-memory
+// slot: the current job (the inner loops read its fields from shared
+// memory, not from the global job list), its index and the next job's first
+// tile, so that a tile of the same job costs one shared-memory load and a
+// comparison, and no registers are held between uses.
+struct JobSlot {
+  LiftJob job;
+  long long next_begin;
+  int ji;
+  int pad_;
+};
+
+struct JobCursor {
+  JobSlot *slot;
+
+  __device__ __forceinline__ void load(LiftParams const &p, int ji,
+                                       int lane) {
+    constexpr int WORDS = sizeof(LiftJob) / 4;
+    static_assert(sizeof(LiftJob) % 4 == 0, "LiftJob is copied in words");
+    unsigned const *src = reinterpret_cast<unsigned const *>(
+        p.jobs != nullptr ? p.jobs + ji : &p.job);
+    __syncwarp();  // every lane is done with the previous job
+    for (int i = lane; i < WORDS; i += 32)
+      reinterpret_cast<unsigned *>(&slot->job)[i] = src[i];
+    if (lane == 0) {
+      slot->ji = ji;
+      slot->next_begin = p.jobs != nullptr && ji + 1 < p.njobs
+                             ? p.jobs[ji + 1].tile_begin
+                             : 0x7fffffffffffffffLL;
+    }
+    __syncwarp();
+  }
+  __device__ __forceinline__ void init(LiftParams const &p, JobSlot *s,
+                                       long long tile, int lane) {
+    slot = s;
+    load(p, p.jobs != nullptr ? find_job(p, tile) : 0, lane);
+  }
+  __device__ __forceinline__ LiftJob const &at(LiftParams const &p,
+                                               long long tile, int lane) {
+    if (tile >= slot->next_begin) {
+      int ji = slot->ji + 1;
+      if (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) {
+        int lo = ji + 1, hi = p.njobs - 1;
+        while (lo < hi) {
+          int const mid = (lo + hi + 1) >> 1;
+          if (p.jobs[mid].tile_begin <= tile)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        ji = lo;
+      }
+      load(p, ji, lane);
+    }
+    return slot->job;
+  }
+};
+
 // Contiguous layout: the thread's elements e = k * R + j (column k, point j)
 // in 16-byte pieces; piece i starts at element i * PER, which lies at
 // k * n + j from the thread's offset (a piece never crosses a column: R is a
@@ -1079,16 +1138,14 @@ __global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
   long long const u0 = T * blockIdx.x / gridDim.x * kTileRounds;
   long long const u1 = T * (blockIdx.x + 1) / gridDim.x * kTileRounds;
   if (u0 >= u1) return;
-  bool const many = p.jobs != nullptr;
   // Job cursors of the copy stream and of the compute stream: both only
   // move forward through the CTA's contiguous range.
-  int jl = many ? find_job(p, u0 / kTileRounds) : 0;
-  int jc = jl;
-  auto job_of = [&](int &ji, long long unit) -> LiftJob const & {
-    if (!many) return p.job;
-    long long const tile = unit / kTileRounds;
-    while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
-    return p.jobs[ji];
+  __shared__ JobSlot wjobs[NT / 32][2];
+  JobCursor jl, jc;
+  jl.init(p, &wjobs[t >> 5][0], u0 / kTileRounds, lane);
+  jc.init(p, &wjobs[t >> 5][1], u0 / kTileRounds, lane);
+  auto job_of = [&](JobCursor &cur, long long unit) -> LiftJob const & {
+    return cur.at(p, unit / kTileRounds, lane);
   };
   auto stage_base = [&](long long unit) {
     return smem_raw + static_cast<int>(unit % S) * (SLOT_BYTES * NT);
@@ -1310,27 +1367,15 @@ __global__ void __launch_bounds__(NT, 2)
   long long const step = Long ? gridDim.x : 1;
   long long const u0 = Long ? blockIdx.x : T * blockIdx.x / gridDim.x;
   long long const u1 = Long ? T : T * (blockIdx.x + 1) / gridDim.x;
-  bool const many = p.jobs != nullptr;
-  int jl = 0, jc = 0;
-  // Job of `tile` (tiles only increase along each cursor): the current job,
-  // the next one, or a binary search over the rest.
-  auto job_of = [&](int &ji, long long tile) -> LiftJob const & {
-    if (!many) return p.job;
-    if (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) {
-      ++ji;
-      if (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) {
-        int lo = ji + 1, hi = p.njobs - 1;
-        while (lo < hi) {
-          int const mid = (lo + hi + 1) >> 1;
-          if (p.jobs[mid].tile_begin <= tile)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-        ji = lo;
-      }
-    }
-    return p.jobs[ji];
+  if (u0 >= u1) return;
+  // Job cursors of the copy stream and of the compute stream (tiles only
+  // increase along each).
+  __shared__ JobSlot wjobs[NT / 32][2];
+  JobCursor jl, jc;
+  jl.init(p, &wjobs[t >> 5][0], u0, lane);
+  jc.init(p, &wjobs[t >> 5][1], u0, lane);
+  auto job_of = [&](JobCursor &cur, long long tile) -> LiftJob const & {
+    return cur.at(p, tile, lane);
   };
   // Element offset of tile column `tc` (a multiple of the piece's columns)
   // in row k; pieces past the job's last column read its last piece.

@@ -169,7 +169,8 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
  * kernel (rows of adjacent columns in registers) on a strided axis and on
  * the last axis, 192 + R and 256 + R the tile kernel (row-major tiles in
  * shared memory, rows of adjacent columns in registers) for pencils of up to
- * 32 chunks and longer ones; `kernels` may be null. Call with
+ * 32 chunks and longer ones, 512 the flat copy of windowed stages' results
+ * back into the grids; `kernels` may be null. Call with
  * capacity 0 to get *nlaunches first. */
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,

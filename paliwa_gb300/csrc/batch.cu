@@ -140,7 +140,9 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
           LiftJob job = st->job;
           job.tile_begin = L.tiles;
           L.tiles += st->tiles;
-          L.points += st->job.columns << st->job.log2_n;
+          L.points += st->R == kCopy
+                          ? st->job.columns / static_cast<long long>(es)
+                          : st->job.columns << st->job.log2_n;
           all_jobs.push_back(job);
         }
         if (L.R != 0 && L.tiles > 0) dr.launches.push_back(L);

@@ -280,16 +280,26 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
     st.tiles = ceil_div(1LL << v.log2_n, seg_len) * st.job.col_tiles;
     out.push_back(st);
     Stage cp;
-    cp.R = R;
     cp.job = make_job(v, shifts, first, 0);
     cp.job.base = v.shadow;
     cp.job.dst_base = v.base;
-    cp.job.periodic = 0;
-    cp.job.log2_window = kWindowLog2;
-    cp.job.seg_len = static_cast<int>(window);
-    cp.job.halo = 0;
-    cp.job.col_tiles = ceil_div(v.columns, C);
-    cp.tiles = ceil_div(1LL << v.log2_n, window) * cp.job.col_tiles;
+    long long const bytes = (v.columns << v.log2_n) << v.log2_es;
+    if (v.log2_kstride == v.log2_inner && v.log2_row > 0 &&
+        v.shadow % 16 == 0 && bytes % 16 == 0) {
+      // The whole grid, contiguous in both buffers: a flat copy.
+      cp.R = kCopy;
+      cp.job.columns = bytes;
+      cp.tiles = ceil_div(bytes, kCopyTileBytes);
+    } else {
+      // A sub-lattice, or unaligned buffers: a window pass without levels.
+      cp.R = R;
+      cp.job.periodic = 0;
+      cp.job.log2_window = kWindowLog2;
+      cp.job.seg_len = static_cast<int>(window);
+      cp.job.halo = 0;
+      cp.job.col_tiles = ceil_div(v.columns, C);
+      cp.tiles = ceil_div(1LL << v.log2_n, window) * cp.job.col_tiles;
+    }
     out.push_back(cp);
     first += count;
   }
@@ -367,6 +377,7 @@ void launch_lift(int dtype, bool exact, bool symmetric, int sched, int R,
   params.total_tiles = total_tiles;
   params.rounds = kRounds;
   if (params.fp64_log2_points >= 0) sched = -1;
+  if (R == kCopy) return launch_copy(params, s);
   if (R > kWide) {  // the wide and tile kernels
     switch (dtype) {
     case PALIWA_GB_F64: return launch_wide_f64(sched, R, params, s);
@@ -567,3 +578,13 @@ int paliwa_gb_dehierarchize(void *grid, int dtype, int ndim,
 }
 
 } // extern "C"
+
+namespace pgb {
+
+void launch_copy(LiftParams const &p, cudaStream_t s) {
+  static thread_local int per_sm = 0;
+  static thread_local int sms = 0;
+  launch_persistent(copy_kernel<kThreads>, 0, p, s, per_sm, sms);
+}
+
+} // namespace pgb

@@ -133,6 +133,7 @@ void launch_lift_f32(bool exact, int sched, int R, LiftParams const &p,
                      cudaStream_t s);
 void launch_lift_f32c(bool exact_sym, int sched, int R, LiftParams const &p,
                       cudaStream_t s);
+void launch_copy(LiftParams const &p, cudaStream_t s);
 void launch_wide_f64(int sched, int code, LiftParams const &p, cudaStream_t s);
 void launch_wide_f32(int sched, int code, LiftParams const &p, cudaStream_t s);
 void launch_wide_f32c(int sched, int code, LiftParams const &p,

@@ -1472,6 +1472,44 @@ __global__ void __launch_bounds__(NT, 2)
   cp_async_wait_all();
 }
 
+// Copy kernel: each job moves `columns` bytes (a multiple of 16, both ends
+// 16-byte aligned) from `base` to `dst_base`; a tile is kCopyTileBytes of
+// one job. It returns the windowed stages' shadow buffer to the grid: a
+// flat copy at HBM speed instead of a lifting pass over windows with no
+// levels.
+constexpr int kCopyTileBytes = 1 << 16;
+
+template <int NT>
+__global__ void __launch_bounds__(NT)
+    copy_kernel(__grid_constant__ const LiftParams p) {
+  constexpr int PER = kCopyTileBytes / 16 / NT;  // 16-byte vectors / thread
+  int const t = threadIdx.x;
+  int const lane = t & 31;
+  __shared__ JobSlot wjobs[NT / 32];
+  JobCursor cur;
+  long long const first = blockIdx.x;
+  if (first >= p.total_tiles) return;
+  cur.init(p, &wjobs[t >> 5], first, lane);
+  for (long long tile = first; tile < p.total_tiles; tile += gridDim.x) {
+    LiftJob const &job = cur.at(p, tile, lane);
+    long long const off = (tile - job.tile_begin) * kCopyTileBytes;
+    long long const left = job.columns - off;  // bytes left in the job
+    uint4 const *src = reinterpret_cast<uint4 const *>(job.base + off);
+    uint4 *dst = reinterpret_cast<uint4 *>(job.dst_base + off);
+    uint4 v[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      long long const b = static_cast<long long>(i * NT + t) * 16;
+      if (b < left) v[i] = src[i * NT + t];
+    }
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      long long const b = static_cast<long long>(i * NT + t) * 16;
+      if (b < left) dst[i * NT + t] = v[i];
+    }
+  }
+}
+
 // Dynamic shared memory of one CTA (an upper bound over every column shape:
 // cols * pitch <= rounds * NT * (R + 1) + cols and cols <= rounds * NT).
 template <class A, int R, int NT>

@@ -68,6 +68,8 @@ constexpr int kWide = 64;
 constexpr int kWideContig = 128;
 constexpr int kTile = 192;
 constexpr int kTileLong = 256;
+// Stage::R of a flat copy (copy_kernel): job.columns counts bytes.
+constexpr int kCopy = 512;
 
 // One stage of an axis transform: a job for one kernel. The stages of one
 // axis must run in order; stages of different grids are independent.

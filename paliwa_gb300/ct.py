@@ -70,6 +70,8 @@ def packed_grids(levels, dtype, device="cuda", align=64):
 
 def kernel_name(code):
     """Name of the lifting kernel behind a launch code of Batch.profile."""
+    if code == 512:
+        return "copy_kernel"
     if code > 256:
         return f"tile_kernel long R={code - 256}"
     if code > 192:

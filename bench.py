@@ -386,6 +386,20 @@ def run_gpu(args, w, world, rank, local):
         bt64 = pct.Batch(v64, w.levels, w.lmin, w.lmax, w.wavelet)
         bt32 = pct.Batch(v32, w.levels, w.lmin, w.lmax, w.wavelet,
                          compensated=True)
+        tuning = None
+        if not args.no_tune:
+            # The library's autotuner picks a kernel per class of stages by
+            # timing each direction; it leaves the grids' contents changed
+            # by rounding, so the inputs are restored after it.
+            t0 = time.time()
+            changed32 = bt32.autotune(reps=2, stream=stream)
+            changed64 = bt64.autotune(reps=2, stream=stream)
+            tuning = {"classes_changed_f32c": changed32,
+                      "classes_changed_f64": changed64,
+                      "seconds": time.time() - t0}
+            b64.copy_(pristine)
+            b32.copy_(pristine)
+            stream.synchronize()
         # Accuracy of the compensated FP32 forward transform against FP64:
         # against the FP64 transform of the FP64 inputs (the headline), and
         # against the FP64 transform of the same FP32-rounded inputs (the
@@ -604,6 +618,7 @@ def run_gpu(args, w, world, rank, local):
                 "all_launches_frac":
                     tot32_b / (tot32_ms / 1e3) / 1e9 / peak},
             "combine": combine,
+            "autotune": tuning,
             "clocks": clocks.summary(),
             "e2e": {"value": e2e_value, "unit": "points/s",
                     "h2d_bytes_per_step": e2e_bytes,
@@ -627,6 +642,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner (the planner's default "
+                         "kernels)")
     ap.add_argument("--launch-table", action="store_true",
                     help="print the plan's launches (kernel, algorithmic "
                          "bytes, event-timed ms) to stderr")

@@ -175,6 +175,29 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,
                             int64_t *bytes, int32_t *kernels);
+/* Autotuner: for each direction, each class of periodic stages (last axis
+ * or strided, sub-lattice or not, pencil length, inner extent) and each
+ * kernel that applies to it (staged, direct, wide, tile), re-plans and times
+ * the whole direction (best of `reps` event-timed runs without a graph) and
+ * keeps the fastest choice; classes are tried one after another (coordinate
+ * descent from the planner's defaults; classes holding under 2 % of the
+ * points are left at the default). Runs the transforms on the batch's
+ * grids: every timed direction is paired with its inverse, so the contents
+ * come back up to rounding (bit-exact for FP64 and FP32 only if the
+ * transform pair is exact on them). Synchronises with the stream. *changed
+ * (may be null) = classes whose kernel changed. Takes a second or more for
+ * a large batch; graphs are re-captured on the next run. No counterpart in
+ * the reference, which has no kernel choice to make. */
+int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,
+                             int *changed);
+/* The classes of periodic stages of one direction's plan: class code
+ * (bit 0 last axis, bit 1 sub-lattice of a long pencil, bits 2-7 log2 of the
+ * pencil length, bits 8-11 log2 of the inner extent in bytes, capped at 8),
+ * the kernels that apply (bit c for c = 0 staged, 1 direct, 2 wide, 3 tile)
+ * and the chosen one. Call with capacity 0 to get *nclasses first. */
+int paliwa_gb_batch_tuning(const paliwa_gb_batch *batch, int forward,
+                           int capacity, int *nclasses, int32_t *classes,
+                           int32_t *kernels, int32_t *choices);
 void paliwa_gb_batch_destroy(paliwa_gb_batch *batch);
 
 /* ------------------------------------------------------------------------

@@ -58,6 +58,10 @@ SIGNATURES = {
         _i, [_vp, _i, _vp, _i, ctypes.POINTER(_i),
              ctypes.POINTER(ctypes.c_float), _pi64,
              ctypes.POINTER(ctypes.c_int32)]),
+    "paliwa_gb_batch_autotune": (_i, [_vp, _vp, _i, ctypes.POINTER(_i)]),
+    "paliwa_gb_batch_tuning": (
+        _i, [_vp, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_int32),
+             ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "paliwa_gb_batch_destroy": (None, [_vp]),
     "paliwa_gb_ct_create": (
         _i, [_i, _i, _pi64, _pd, _pi64, _i, ctypes.POINTER(_vp), _i,

@@ -41,6 +41,15 @@ struct Direction {
   LiftJob *jobs_dev = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
+  Tuning tuning;  // kernel forced per class (autotuner)
+  // Classes of the plan's periodic stages: applicable kernels (bits), the
+  // default choice of the first stage seen, and the points they store.
+  struct ClassInfo {
+    unsigned kernels = 0;
+    int dflt = 0;
+    long long points = 0;
+  };
+  std::map<int, ClassInfo> classes;
 };
 
 void free_direction(Direction &d) {
@@ -48,6 +57,8 @@ void free_direction(Direction &d) {
   if (d.jobs_dev) cudaFree(d.jobs_dev);
   d.graph = nullptr;
   d.jobs_dev = nullptr;
+  d.launches.clear();
+  d.classes.clear();
 }
 
 void check_grid_levels(int ndim, int ngrids, int64_t const *levels,
@@ -82,6 +93,9 @@ struct paliwa_gb_batch {
   long long points = 0;
   bool use_graphs = true;
   Direction dir[2];  // 0 = forward, 1 = inverse
+  // The grids as created (for re-planning).
+  std::vector<int64_t> levels, lmin;
+  std::vector<void *> grids;
   // Shadow buffers of the windowed stages (grids with pencils longer than
   // one CTA holds), reused by every axis: one direction runs at a time.
   void *shadow = nullptr;
@@ -119,7 +133,16 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
             reinterpret_cast<unsigned long long>(b.shadow) + shadow_off;
         shadow_off += (bytes + 255) / 256 * 256;
       }
-      plan_axis(view, shifts, filters, stages[g]);
+      plan_axis(view, shifts, filters, stages[g], &dr.tuning);
+      for (Stage const &st : stages[g]) {
+        if (st.kernels == 0) continue;
+        auto &ci = dr.classes[st.tclass];
+        if (ci.kernels == 0) {
+          ci.kernels = st.kernels;
+          ci.dflt = st.dflt;
+        }
+        ci.points += st.job.columns << st.job.log2_n;
+      }
       depth = std::max(depth, stages[g].size());
     }
     for (size_t k = 0; k < depth; ++k) {
@@ -350,6 +373,9 @@ int paliwa_gb_batch_create(int ndim, int ngrids, const int64_t *levels,
     b->ngrids = ngrids;
     b->dtype = dtype;
     b->wavelet = wavelet;
+    b->levels.assign(levels, levels + static_cast<size_t>(ngrids) * ndim);
+    b->lmin.assign(minimum_level, minimum_level + ndim);
+    b->grids.assign(grid_ptrs, grid_ptrs + ngrids);
     for (int g = 0; g < ngrids; ++g) {
       if (grid_ptrs[g] == nullptr ||
           reinterpret_cast<uintptr_t>(grid_ptrs[g]) % es != 0)
@@ -423,6 +449,118 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
       *launches_forward = static_cast<int64_t>(batch->dir[0].launches.size());
     if (launches_inverse)
       *launches_inverse = static_cast<int64_t>(batch->dir[1].launches.size());
+  });
+}
+
+namespace {
+
+// Milliseconds of direction `which` (0 forward, 1 inverse), best of `reps`
+// event-timed runs without a graph; every run is followed (forward) or
+// preceded (inverse) by the other direction, so that the grids return to
+// their contents up to rounding.
+float time_direction(paliwa_gb_batch &b, int which, int reps,
+                     cudaStream_t s) {
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+  auto run = [&](Direction &dr) {
+    for (auto const &L : dr.launches)
+      launch_lift(b.dtype, dr.exact, dr.symmetric, L.sched, L.R, dr.params,
+                  dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
+  };
+  float best = 1e30f;
+  for (int r = 0; r < reps; ++r) {
+    if (which == 1) run(b.dir[0]);
+    cuda_check(cudaEventRecord(e0, s), "cudaEventRecord");
+    run(b.dir[which]);
+    cuda_check(cudaEventRecord(e1, s), "cudaEventRecord");
+    if (which == 0) run(b.dir[1]);
+    cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    float ms = 0;
+    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
+void replan(paliwa_gb_batch &b, int which) {
+  Direction &dr = b.dir[which];
+  free_direction(dr);
+  plan_direction(b, dr, which == 0, b.levels.data(), b.lmin.data(),
+                 b.grids.data());
+}
+
+} // namespace
+
+int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,
+                             int *changed) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    if (reps < 1) reps = 1;
+    cudaStream_t const s = static_cast<cudaStream_t>(stream);
+    int nchanged = 0;
+    for (int which = 0; which < 2; ++which) {
+      Direction &dr = batch->dir[which];
+      // Coordinate descent over the classes of periodic stages: try every
+      // kernel that applies to a class, keep the fastest whole direction.
+      auto const classes = dr.classes;
+      long long total = 0;
+      for (auto const &kv : classes) total += kv.second.points;
+      float best = time_direction(*batch, which, reps, s);
+      for (auto const &[tclass, info] : classes) {
+        unsigned const mask = info.kernels;
+        int const dflt = info.dflt;
+        if ((mask & (mask - 1)) == 0) continue;  // one kernel applies
+        // A class with under 2 % of the points cannot move the direction's
+        // time by the 1 % a change must gain.
+        if (info.points * 50 < total) continue;
+        auto const it = dr.tuning.choice.find(tclass);
+        int const current = it != dr.tuning.choice.end() ? it->second : dflt;
+        int keep = current;
+        for (int c = 0; c < kChooseCount; ++c) {
+          if (c == current || !((mask >> c) & 1u)) continue;
+          dr.tuning.choice[tclass] = c;
+          replan(*batch, which);
+          float const t = time_direction(*batch, which, reps, s);
+          if (t < best * 0.99f) {
+            best = t;
+            keep = c;
+          }
+        }
+        if (keep == dflt && it == dr.tuning.choice.end())
+          dr.tuning.choice.erase(tclass);
+        else
+          dr.tuning.choice[tclass] = keep;
+        if (keep != current) ++nchanged;
+        replan(*batch, which);
+      }
+    }
+    if (changed != nullptr) *changed = nchanged;
+  });
+}
+
+int paliwa_gb_batch_tuning(const paliwa_gb_batch *batch, int forward,
+                           int capacity, int *nclasses, int32_t *classes,
+                           int32_t *kernels, int32_t *choices) {
+  return guarded([&] {
+    if (batch == nullptr || nclasses == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    Direction const &dr = batch->dir[forward ? 0 : 1];
+    *nclasses = static_cast<int>(dr.classes.size());
+    if (capacity < *nclasses || classes == nullptr || kernels == nullptr ||
+        choices == nullptr)
+      return;
+    int i = 0;
+    for (auto const &[tclass, info] : dr.classes) {
+      auto const it = dr.tuning.choice.find(tclass);
+      classes[i] = tclass;
+      kernels[i] = static_cast<int32_t>(info.kernels);
+      choices[i] = it != dr.tuning.choice.end() ? it->second : info.dflt;
+      ++i;
+    }
   });
 }
 

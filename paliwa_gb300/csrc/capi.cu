@@ -170,17 +170,77 @@ LiftJob make_job(AxisView const &v, std::vector<int> const &sh, size_t first,
   return job;
 }
 
+} // namespace
+
+// Kernels that can run the periodic stages of view `v` (a bit per
+// KernelChoice), and the one chosen by default. Applicability: the wide and
+// tile kernels need a wavelet schedule (canonical level range) and a grid
+// aligned to 16 bytes; the wide kernel takes strided pencils of up to 64
+// points whose inner extent holds a row vector, and last-axis pencils of up
+// to 512 points when there is a row vector's worth of them; the tile kernel
+// strided pencils of 128 to 4096 points whose inner extent holds whole copy
+// pieces; the direct kernel pencils that one thread holds whole and
+// last-axis pencils of up to 32 chunks; the staged kernel everything with
+// chunks of 16 points.
+KernelSet periodic_kernels(AxisView const &v, bool canon) {
+  int const R = chunk_for(v.log2_n);
+  int const log2G = v.log2_n - (31 - __builtin_clz(R));
+  bool const aligned = canon && v.log2_row > 0;
+  bool const last = v.log2_inner == 0 && v.log2_kstride == 0;
+  KernelSet k;
+  if (R == 16) k.mask |= 1 << kChooseStaged;
+  if (R == (1 << v.log2_n) || (last && log2G <= 5))
+    k.mask |= 1 << kChooseDirect;
+  if (aligned && ((!last && wide_chunk(v.log2_n) > 0 &&
+                   v.log2_inner >= v.log2_row) ||
+                  (last && log2G <= 5 && v.columns >= (1LL << v.log2_row))))
+    k.mask |= 1 << kChooseWide;
+  if (aligned && !last && R == 16 && log2G >= 3 && log2G <= 8 &&
+      v.log2_inner + v.log2_es >=
+          tile_piece_log2(log2G, v.log2_row + v.log2_es))
+    k.mask |= 1 << kChooseTile;
+  // Default: the wide kernel for strided pencils (and FP32c last-axis
+  // pencils: measured on 2^26-point grids, 3.0-4.5 TB/s against 2.8-4.1 on
+  // the direct kernel), then the tile kernel up to the length where it was
+  // measured faster than the staged kernel (first axis of 2^26-point grids,
+  // and the 4D CT batch): 4096 points in FP32 (2.8 against 1.8 TB/s at
+  // 1024), 512 in FP64, 256 in FP32c (at G = 32 its 8-byte row vectors need
+  // 8-byte copy pieces, and beyond 32 chunks the batch ran slower than on
+  // the staged kernel); then the direct kernel, then the staged one.
+  int const tile_log2G_max = v.wide_last ? 4 : v.log2_es == 3 ? 5 : 8;
+  if (k.has(kChooseWide) && (!last || v.wide_last))
+    k.dflt = kChooseWide;
+  else if (k.has(kChooseTile) && log2G <= tile_log2G_max)
+    k.dflt = kChooseTile;
+  else if (k.has(kChooseDirect))
+    k.dflt = kChooseDirect;
+  else
+    k.dflt = kChooseStaged;
+  return k;
+}
+
+int tuning_class(AxisView const &v) {
+  bool const last = v.log2_inner == 0 && v.log2_kstride == 0;
+  bool const sub = v.log2_kstride != v.log2_inner;
+  int const inner_bytes = std::min(v.log2_inner + v.log2_es, 8);
+  return (last ? 1 : 0) | (sub ? 2 : 0) | (v.log2_n << 2) |
+         (inner_bytes << 8);
+}
+
+namespace {
+
 // Periodic whole-pencil stages; level lists longer than one job holds are
 // split into consecutive stages (order preserved). `ws` is the wavelet
-// schedule of the filters (or -1).
+// schedule of the filters (or -1); `tuning` may force a kernel per class.
 void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
-                   std::vector<Stage> &out) {
+                   Tuning const *tuning, std::vector<Stage> &out) {
   int const R = chunk_for(v.log2_n);
   int const log2G = v.log2_n - (31 - __builtin_clz(R));
   long long const C = static_cast<long long>(kRounds) * (kThreads >> log2G);
   int const wR = wide_chunk(v.log2_n);
   int const wlog2G = wR > 0 ? v.log2_n - (31 - __builtin_clz(wR)) : 0;
   long long const wC = static_cast<long long>(kRounds) * (kThreads >> wlog2G);
+  bool const last = v.log2_inner == 0 && v.log2_kstride == 0;
   for (size_t first = 0; first < shifts.size(); first += kMaxLevels) {
     size_t const count =
         std::min(shifts.size() - first, static_cast<size_t>(kMaxLevels));
@@ -188,47 +248,40 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
     st.job = make_job(v, shifts, first, count);
     st.job.periodic = 1;
     st.job.log2_window = v.log2_n;
-    // The wide kernel (wavelet schedules on grids aligned to 16 bytes):
-    // strided pencils of up to 64 points whose rows hold a whole row vector
-    // of adjacent columns, and (FP32 compensated) last-axis pencils of up to
-    // 512 points when there are at least a row vector's worth of them
-    // (measured on 2^26-point grids, FP32c last axis: 3.0-4.5 TB/s against
-    // 2.8-4.1 on the direct kernel). Otherwise pencils
-    // that one thread holds whole, and last-axis pencils that fit one warp,
-    // run on the direct kernel; the rest staged.
-    bool const canon = ws >= 0 && v.log2_row > 0 &&
-                       canonical_shifts(st.job, (ws & 1) != 0);
-    bool const last = v.log2_inner == 0 && v.log2_kstride == 0;
-    bool const wide = canon && wR > 0 && !last &&
-                      v.log2_inner >= v.log2_row;
-    bool const wide_last = canon && last && v.wide_last && log2G <= 5 &&
-                           v.columns >= (1LL << v.log2_row);
-    bool const direct = R == (1 << v.log2_n) || (last && log2G <= 5);
-    // Strided pencils of 128 points and more whose inner extent holds whole
-    // copy pieces run on the tile kernel, up to the length where it was
-    // measured faster than the staged kernel (first axis of 2^26-point
-    // grids, and the 4D CT batch): 4096 points in FP32 (2.8 against 1.8
-    // TB/s at 1024), 512 in FP64, 256 in FP32c (at G = 32 its 8-byte row
-    // vectors need 8-byte copy pieces, and beyond 32 chunks the batch ran
-    // slower than on the staged kernel).
-    int const tile_log2G_max = v.wide_last ? 4 : v.log2_es == 3 ? 5 : 8;
-    bool const tile = canon && !last && R == 16 && log2G >= 3 &&
-                      log2G <= tile_log2G_max &&
-                      v.log2_inner + v.log2_es >=
-                          tile_piece_log2(log2G, v.log2_row + v.log2_es);
-    if (tile) {
+    bool const canon = ws >= 0 && canonical_shifts(st.job, (ws & 1) != 0);
+    KernelSet const ks = periodic_kernels(v, canon);
+    st.tclass = tuning_class(v);
+    st.kernels = ks.mask;
+    st.dflt = ks.dflt;
+    int choice = ks.dflt;
+    if (tuning != nullptr) {
+      auto const it = tuning->choice.find(tuning_class(v));
+      if (it != tuning->choice.end() && ks.has(it->second))
+        choice = it->second;
+    }
+    switch (choice) {
+    case kChooseWide:
+      if (last) {
+        st.R = kWideContig + R;
+        st.job.col_tiles = ceil_div(v.columns >> v.log2_row, C);
+      } else {
+        st.R = kWide + wR;
+        st.job.col_tiles = ceil_div(v.columns >> v.log2_row, wC);
+      }
+      break;
+    case kChooseTile:
       st.R = (log2G <= 5 ? kTile : kTileLong) + 16;
       st.job.col_tiles =
           ceil_div(v.columns >> v.log2_row, kThreads >> log2G);
-    } else if (wide) {
-      st.R = kWide + wR;
-      st.job.col_tiles = ceil_div(v.columns >> v.log2_row, wC);
-    } else if (wide_last) {
-      st.R = kWideContig + R;
-      st.job.col_tiles = ceil_div(v.columns >> v.log2_row, C);
-    } else {
-      st.R = direct ? -R : R;
+      break;
+    case kChooseDirect:
+      st.R = -R;
       st.job.col_tiles = ceil_div(v.columns, C);
+      break;
+    default:
+      st.R = R;
+      st.job.col_tiles = ceil_div(v.columns, C);
+      break;
     }
     st.tiles = st.job.col_tiles;
     out.push_back(st);
@@ -308,10 +361,11 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
 } // namespace
 
 void plan_axis(AxisView const &view, std::vector<int> const &shifts,
-               std::vector<Filter> const &filters, std::vector<Stage> &out) {
+               std::vector<Filter> const &filters, std::vector<Stage> &out,
+               Tuning const *tuning) {
   if (shifts.empty() || filters.empty() || view.log2_n == 0) return;
   if (view.log2_n <= kWindowLog2) {
-    plan_periodic(view, shifts, wavelet_schedule(filters), out);
+    plan_periodic(view, shifts, wavelet_schedule(filters), tuning, out);
     return;
   }
   // Long pencil: levels closer than 2^m run on windows with a halo of at most
@@ -334,7 +388,7 @@ void plan_axis(AxisView const &view, std::vector<int> const &shifts,
       sub.log2_n = view.log2_n - m;
       sub.log2_kstride = view.log2_kstride + m;
       for (int &s : run) s -= m;
-      plan_axis(sub, run, filters, out);
+      plan_axis(sub, run, filters, out, tuning);
     }
     i = j;
   }

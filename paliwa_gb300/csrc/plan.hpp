@@ -11,6 +11,7 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -77,6 +78,11 @@ struct Stage {
   int R = 0;
   long long tiles = 0;
   LiftJob job{};
+  // Periodic stages: the tuning class and the kernels that apply (a bit per
+  // KernelChoice); 0 for windowed and copy stages.
+  int tclass = 0;
+  unsigned kernels = 0;
+  int dflt = 0;
 };
 
 constexpr int kWindowLog2 = 12;   // points per column per CTA round (4096)
@@ -85,8 +91,31 @@ constexpr int kRounds = kTileRounds;  // column rounds per tile
 constexpr int kHaloBudget = 256;  // halo per side of a window, in points
 
 int chunk_for(int log2_n);        // R for a periodic pencil of 2^log2_n
+
+// Kernel choices for periodic stages, and a table that forces one per class
+// of stage (tuning_class: last axis, sub-lattice, log2 n, inner extent in
+// bytes). A forced kernel that does not apply to a stage is ignored.
+enum KernelChoice {
+  kChooseStaged = 0,
+  kChooseDirect = 1,
+  kChooseWide = 2,
+  kChooseTile = 3,
+  kChooseCount = 4
+};
+struct KernelSet {
+  unsigned mask = 0;  // a bit per applicable KernelChoice
+  int dflt = kChooseStaged;
+  bool has(int c) const { return (mask >> c) & 1u; }
+};
+struct Tuning {
+  std::map<int, int> choice;  // tuning_class -> KernelChoice
+};
+KernelSet periodic_kernels(AxisView const &v, bool canonical);
+int tuning_class(AxisView const &v);
+
 void plan_axis(AxisView const &view, std::vector<int> const &shifts,
-               std::vector<Filter> const &filters, std::vector<Stage> &out);
+               std::vector<Filter> const &filters, std::vector<Stage> &out,
+               Tuning const *tuning = nullptr);
 
 // True when planning `view` along `shifts` needs a shadow buffer.
 inline bool needs_shadow(AxisView const &view, std::vector<int> const &shifts) {

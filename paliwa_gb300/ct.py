@@ -160,6 +160,38 @@ class Batch:
             self._h, int(forward), s, n.value, ctypes.byref(n), ms, by, kd))
         return (list(ms[:n.value]), list(by[:n.value]), list(kd[:n.value]))
 
+    def autotune(self, reps=2, stream=None):
+        """Pick the fastest kernel per class of stages by timing each
+        direction (see paliwa_gb_batch_autotune); returns the number of
+        classes whose kernel changed. The grids' contents come back up to
+        rounding."""
+        n = ctypes.c_int()
+        _lib.check(self._lib.paliwa_gb_batch_autotune(
+            self._h, _stream_handle(self.grids[0], stream), int(reps),
+            ctypes.byref(n)))
+        return n.value
+
+    KERNELS = ("staged", "direct", "wide", "tile")
+
+    def tuning(self, forward=True):
+        """[(class, {last, sub, log2_n, log2_inner_bytes}, applicable kernel
+        names, chosen kernel name)] of one direction's plan."""
+        n = ctypes.c_int()
+        _lib.check(self._lib.paliwa_gb_batch_tuning(
+            self._h, int(forward), 0, ctypes.byref(n), None, None, None))
+        cl = (ctypes.c_int32 * max(1, n.value))()
+        ks = (ctypes.c_int32 * max(1, n.value))()
+        ch = (ctypes.c_int32 * max(1, n.value))()
+        _lib.check(self._lib.paliwa_gb_batch_tuning(
+            self._h, int(forward), n.value, ctypes.byref(n), cl, ks, ch))
+        out = []
+        for c, k, x in zip(cl[:n.value], ks[:n.value], ch[:n.value]):
+            desc = {"last": c & 1, "sub": (c >> 1) & 1,
+                    "log2_n": (c >> 2) & 63, "log2_inner_bytes": c >> 8}
+            names = [self.KERNELS[i] for i in range(4) if (k >> i) & 1]
+            out.append((c, desc, names, self.KERNELS[x]))
+        return out
+
     def close(self):
         if self._h:
             self._lib.paliwa_gb_batch_destroy(self._h)

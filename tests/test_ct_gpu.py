@@ -293,3 +293,46 @@ def test_host_batch_matches_device_batch():
         assert torch.equal(buf.cpu(), host_out), steps
         b.close()
     hb.close()
+
+
+def test_autotune_keeps_results_exact():
+    """After the autotuner has re-planned (any kernel per class of stages),
+    FP64 stays bit-identical to the oracle and FP32c to the compensated
+    model; the tuning report names an applicable kernel for every class."""
+    import torch
+    from compensated import hierarchize as model
+    levels, _ = pct.combination_scheme(4, 13, 3, 1)
+    lmin, lmax = (1, 1, 1, 1), (10, 10, 10, 10)
+    rng = np.random.default_rng(17)
+    O = oracle()
+    for dt, comp in ((torch.float64, False), (torch.float32, True)):
+        buf, gs = pct.packed_grids(levels, dt)
+        x = rng.uniform(-1, 1, buf.numel())
+        buf.copy_(torch.from_numpy(x))
+        pristine = buf.clone()
+        s = torch.cuda.Stream()
+        b = pct.Batch(gs, levels, lmin, lmax, "biorthogonal", compensated=comp)
+        b.autotune(reps=1, stream=s)
+        for fwd in (True, False):
+            rep = b.tuning(fwd)
+            assert rep
+            for _, desc, names, chosen in rep:
+                assert chosen in names, (desc, names, chosen)
+        buf.copy_(pristine)
+        torch.cuda.synchronize()
+        b.hierarchize(s)
+        s.synchronize()
+        for i in range(0, len(levels), 7):
+            lv = levels[i]
+            shape = [1 << l for l in lv]
+            o = (gs[i].data_ptr() - buf.data_ptr()) // buf.element_size()
+            xi = pristine[o:o + gs[i].numel()].cpu().numpy().reshape(shape)
+            got = gs[i].cpu().numpy().reshape(shape)
+            if comp:
+                want = model(xi, lv, lmin, "biorthogonal", True)
+                assert np.array_equal(got.view(np.uint32),
+                                      want.view(np.uint32)), lv
+            else:
+                want = O.hierarchize(xi.copy(), lv, lmin, lmax, "biorthogonal")
+                assert np.array_equal(got, want), lv
+        b.close()

@@ -135,3 +135,17 @@ def test_compensated_model_close_to_fp64(oracle_mod, wavelet):
         assert err <= 1e-6, err
         # One rounding per axis and point: at most 3 ulps-scale errors.
         assert err <= 3 * 2.0 ** -24 * 1.01 + 1e-12 or err < err_plain
+
+
+def test_c1_configuration_round_trip(oracle_mod):
+    """C1, the reference's CPU-sized case: 2D hat at (6, 6) on
+    sin(2 pi x) cos(3 pi y) + noise; the forward keeps the lmin = 0 point
+    (hat, paliwa test_paliwa_transform.cpp:57-73 style) and the round trip
+    returns the input to 1e-13."""
+    x = np.arange(64) / 64.0
+    f = np.multiply.outer(np.sin(2 * np.pi * x), np.cos(3 * np.pi * x))
+    f = f + np.random.default_rng(20261204).uniform(-0.01, 0.01, f.shape)
+    h = oracle_mod.hierarchize(f.copy(), (6, 6), (0, 0), (6, 6), "hat")
+    assert h[0, 0] == f[0, 0]
+    back = oracle_mod.dehierarchize(h, (6, 6), (0, 0), (6, 6), "hat")
+    assert np.max(np.abs(back - f)) <= 1e-13 * np.max(np.abs(f))

@@ -773,10 +773,24 @@ template <typename S, int R, int NT> struct TileCopy {
   }
 };
 
-// Direct: every job of the launch is a periodic pencil of n == R points held
-// by one thread (no staging); otherwise tiles are staged through shared
-// memory. The two paths are separate instantiations so that neither's
-// register budget constrains the other.
+// Moves a job cursor forward to the last job that starts at or before
+// `tile`. The jobs after ji are examined 32 at a time, one per lane, with
+// independent loads (tile_begin increases along the list, so the jobs that
+// start at or before `tile` form a prefix). CTAs that take every
+// gridDim.x-th tile step over many small jobs per tile; one job per step
+// would be a chain of dependent loads per tile. Called by all lanes of the
+// warp with the same tile.
+__device__ __forceinline__ int advance_job(LiftParams const &p, int ji,
+                                           long long tile, int lane) {
+  for (;;) {
+    int const j = ji + 1 + lane;
+    bool const ok = j < p.njobs && p.jobs[j].tile_begin <= tile;
+    unsigned const m = __ballot_sync(0xffffffffu, ok);
+    ji += __popc(m);
+    if (m != 0xffffffffu) return ji;
+  }
+}
+
 // Moves the job cursor `ji` forward to the job of `tile` and copies that job
 // into shared memory when it changed. Called by every thread of the CTA.
 // The current job lives in shared memory: its fields are read in the inner
@@ -786,8 +800,7 @@ template <int NT>
 __device__ __forceinline__ void fetch_job(LiftParams const &p, long long tile,
                                           int t, int &ji, LiftJob &sjob,
                                           int &sjob_index) {
-  if (p.jobs != nullptr)
-    while (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) ++ji;
+  if (p.jobs != nullptr) ji = advance_job(p, ji, tile, t & 31);
   if (sjob_index != ji) {
     __syncthreads();  // every thread has read sjob_index
     constexpr int WORDS = sizeof(LiftJob) / 4;
@@ -801,6 +814,10 @@ __device__ __forceinline__ void fetch_job(LiftParams const &p, long long tile,
   }
 }
 
+// Direct: every job of the launch is a periodic pencil of n == R points held
+// by one thread (no staging); otherwise tiles are staged through shared
+// memory. The two paths are separate instantiations so that neither's
+// register budget constrains the other.
 template <class A, int R, int NT, class Sched, bool Direct>
 __global__ void __launch_bounds__(NT)
     lift_kernel(__grid_constant__ const LiftParams p) {
@@ -1043,21 +1060,8 @@ struct JobCursor {
   }
   __device__ __forceinline__ LiftJob const &at(LiftParams const &p,
                                                long long tile, int lane) {
-    if (tile >= slot->next_begin) {
-      int ji = slot->ji + 1;
-      if (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile) {
-        int lo = ji + 1, hi = p.njobs - 1;
-        while (lo < hi) {
-          int const mid = (lo + hi + 1) >> 1;
-          if (p.jobs[mid].tile_begin <= tile)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-        ji = lo;
-      }
-      load(p, ji, lane);
-    }
+    if (tile >= slot->next_begin)
+      load(p, advance_job(p, slot->ji, tile, lane), lane);
     return slot->job;
   }
 };

@@ -72,6 +72,12 @@ int tile_piece_log2(int log2G, int log2_row_bytes) {
   return (pad & 15) != 0 || log2rb < 4 ? 3 : 4;
 }
 
+// Points per thread of the staged kernel: 16, or 32 for FP32c pencils of
+// 1024 points and more (and their windows).
+int staged_chunk(AxisView const &v) {
+  return v.wide_last && v.log2_n >= 10 ? 32 : 16;
+}
+
 int wide_chunk(int log2_n) {
   if (log2_n <= 4) return 1 << log2_n;
   if (log2_n <= 6) return 1 << (log2_n - 2);
@@ -278,10 +284,16 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
       st.R = -R;
       st.job.col_tiles = ceil_div(v.columns, C);
       break;
-    default:
-      st.R = R;
-      st.job.col_tiles = ceil_div(v.columns, C);
+    default: {
+      // FP32c pencils of 1024 points and more hold 32 points per thread:
+      // half the chunks to exchange through shared memory.
+      int const sR = staged_chunk(v);
+      int const slog2G = v.log2_n - (31 - __builtin_clz(sR));
+      st.R = sR;
+      st.job.col_tiles = ceil_div(
+          v.columns, static_cast<long long>(kRounds) * (kThreads >> slog2G));
       break;
+    }
     }
     st.tiles = st.job.col_tiles;
     out.push_back(st);
@@ -293,9 +305,11 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
                   std::vector<Filter> const &filters,
                   std::vector<Stage> &out) {
   long long const window = 1LL << kWindowLog2;
-  int const R = 16;
-  long long const C =
-      static_cast<long long>(kRounds) * (kThreads >> (kWindowLog2 - 4));
+  AxisView wv = v;
+  wv.log2_n = kWindowLog2;
+  int const R = staged_chunk(wv);
+  long long const C = static_cast<long long>(kRounds) *
+                      (kThreads >> (kWindowLog2 - (31 - __builtin_clz(R))));
   size_t first = 0;
   while (first < shifts.size()) {
     // Grow the run while the halo it needs fits the window: each step of

@@ -106,6 +106,7 @@ void launch_sched(int R, LiftParams const &p, cudaStream_t s) {
   case -8: return launch_r<A, 8, Sched, true>(p, s);
   case -16: return launch_r<A, 16, Sched, true>(p, s);
   case 16: return launch_r<A, 16, Sched, false>(p, s);
+  case 32: return launch_r<A, 32, Sched, false>(p, s);
   }
   throw StatusError(2, "bad chunk size");
 }

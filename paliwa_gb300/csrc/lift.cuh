@@ -498,12 +498,63 @@ template <int W, bool FWD> struct WaveletSched {
     if ((step > 0 && sh_first > sh_last) || (step < 0 && sh_first < sh_last))
       return;
     V s0[1] = {{f2_x(q[0].h), f2_x(q[0].l)}};
-    for (int sh = sh_first;; sh += step) {
-      coarse_level<A, 1, NT>(s0, ctx, 1 << (sh - LOG2R), Passes{});
-      if (sh == sh_last) break;
+    if (!coarse_heads<A, R, NT>(s0[0], ctx, (step > 0 ? sh_last : sh_first) -
+                                               LOG2R + 1)) {
+      for (int sh = sh_first;; sh += step) {
+        coarse_level<A, 1, NT>(s0, ctx, 1 << (sh - LOG2R), Passes{});
+        if (sh == sh_last) break;
+      }
     }
     q[0].h = f2_pack(s0[0].h, f2_y(q[0].h));
     q[0].l = f2_pack(s0[0].l, f2_y(q[0].l));
+  }
+
+  // The coarse levels of pencils of more than 32 chunks (staged kernel,
+  // chunks in consecutive threads): instead of one shared-memory exchange
+  // and barrier per level pass, the chunk heads go to shared memory once,
+  // one warp per column runs all Lc coarse levels on its column's G heads as
+  // a pencil of 32 chunks of G / 32 heads (shuffles only: the same updates
+  // in the same order), and the heads come back. Returns false (nothing
+  // done) when the pencil has at most 32 chunks. Called by every thread.
+  template <int K, class A, int NT>
+  static __device__ __forceinline__ void head_pencil(typename A::V *col,
+                                                     int lane, int periodic,
+                                                     int Lc) {
+    using V = typename A::V;
+    V hv[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) hv[k] = col[lane * K + k];
+    RoundCtx<A, NT> hctx(lane, lane, 32, 5, lane, periodic, nullptr, nullptr);
+    run_levels<A, K, NT>(hv, hctx, Lc);
+#pragma unroll
+    for (int k = 0; k < K; ++k) col[lane * K + k] = hv[k];
+  }
+  template <class A, int R, int NT>
+  static __device__ __forceinline__ bool coarse_heads(typename A::V &head,
+                                                      RoundCtx<A, NT> &ctx,
+                                                      int Lc) {
+    if constexpr (R < 16) {
+      return false;
+    } else {
+      if (ctx.G <= 32 || ctx.G > 256) return false;
+      using V = typename A::V;
+      ctx.heads[ctx.t] = head;
+      __syncthreads();
+      int const w = ctx.t >> 5;
+      int const lane = ctx.t & 31;
+      if (w < (NT >> ctx.log2G)) {  // one warp per column of the round
+        V *const col = ctx.heads + (w << ctx.log2G);
+        switch (ctx.G) {
+        case 64: head_pencil<2, A, NT>(col, lane, ctx.periodic, Lc); break;
+        case 128: head_pencil<4, A, NT>(col, lane, ctx.periodic, Lc); break;
+        case 256: head_pencil<8, A, NT>(col, lane, ctx.periodic, Lc); break;
+        }
+      }
+      __syncthreads();
+      head = ctx.heads[ctx.t];
+      ctx.heads_valid = false;
+      return true;
+    }
   }
 
   template <class A, int R, int NT>
@@ -544,11 +595,13 @@ template <int W, bool FWD> struct WaveletSched {
     }
     if constexpr (FWD) {
       fine_up<A, R, NT, 0>(v, ctx, L);
-      for (int sh = LOG2R; sh < L; ++sh)
-        coarse_level<A, R, NT>(v, ctx, 1 << (sh - LOG2R), Passes{});
+      if (L <= LOG2R || !coarse_heads<A, R, NT>(v[0], ctx, L - LOG2R))
+        for (int sh = LOG2R; sh < L; ++sh)
+          coarse_level<A, R, NT>(v, ctx, 1 << (sh - LOG2R), Passes{});
     } else {
-      for (int sh = L - 1; sh >= LOG2R; --sh)
-        coarse_level<A, R, NT>(v, ctx, 1 << (sh - LOG2R), Passes{});
+      if (L <= LOG2R || !coarse_heads<A, R, NT>(v[0], ctx, L - LOG2R))
+        for (int sh = L - 1; sh >= LOG2R; --sh)
+          coarse_level<A, R, NT>(v, ctx, 1 << (sh - LOG2R), Passes{});
       fine_down<A, R, NT, LOG2R - 1>(v, ctx, L);
     }
   }

@@ -193,8 +193,9 @@ int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,
 /* The classes of periodic stages of one direction's plan: class code
  * (bit 0 last axis, bit 1 sub-lattice of a long pencil, bits 2-7 log2 of the
  * pencil length, bits 8-11 log2 of the inner extent in bytes, capped at 8),
- * the kernels that apply (bit c for c = 0 staged, 1 direct, 2 wide, 3 tile)
- * and the chosen one. Call with capacity 0 to get *nclasses first. */
+ * the kernels that apply (bit c for c = 0 staged with 16-point chunks,
+ * 1 direct, 2 wide, 3 tile, 4 staged with 32-point chunks) and the chosen
+ * one. Call with capacity 0 to get *nclasses first. */
 int paliwa_gb_batch_tuning(const paliwa_gb_batch *batch, int forward,
                            int capacity, int *nclasses, int32_t *classes,
                            int32_t *kernels, int32_t *choices);

@@ -198,6 +198,7 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   bool const last = v.log2_inner == 0 && v.log2_kstride == 0;
   KernelSet k;
   if (R == 16) k.mask |= 1 << kChooseStaged;
+  if (v.log2_n >= 6) k.mask |= 1 << kChooseStaged32;
   if (R == (1 << v.log2_n) || (last && log2G <= 5))
     k.mask |= 1 << kChooseDirect;
   if (aligned && ((!last && wide_chunk(v.log2_n) > 0 &&
@@ -224,7 +225,7 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   else if (k.has(kChooseDirect))
     k.dflt = kChooseDirect;
   else
-    k.dflt = kChooseStaged;
+    k.dflt = staged_chunk(v) == 32 ? kChooseStaged32 : kChooseStaged;
   return k;
 }
 
@@ -288,9 +289,7 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
       st.job.col_tiles = ceil_div(v.columns, C);
       break;
     default: {
-      // FP32c pencils of 1024 points and more hold 32 points per thread:
-      // half the chunks to exchange through shared memory.
-      int const sR = staged_chunk(v);
+      int const sR = choice == kChooseStaged32 ? 32 : R;
       int const slog2G = v.log2_n - (31 - __builtin_clz(sR));
       st.R = sR;
       st.job.col_tiles = ceil_div(

@@ -96,11 +96,12 @@ int chunk_for(int log2_n);        // R for a periodic pencil of 2^log2_n
 // of stage (tuning_class: last axis, sub-lattice, log2 n, inner extent in
 // bytes). A forced kernel that does not apply to a stage is ignored.
 enum KernelChoice {
-  kChooseStaged = 0,
+  kChooseStaged = 0,    // staged, 16 points per thread (or n when shorter)
   kChooseDirect = 1,
   kChooseWide = 2,
   kChooseTile = 3,
-  kChooseCount = 4
+  kChooseStaged32 = 4,  // staged, 32 points per thread
+  kChooseCount = 5
 };
 struct KernelSet {
   unsigned mask = 0;  // a bit per applicable KernelChoice

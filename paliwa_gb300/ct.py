@@ -171,7 +171,7 @@ class Batch:
             ctypes.byref(n)))
         return n.value
 
-    KERNELS = ("staged", "direct", "wide", "tile")
+    KERNELS = ("staged", "direct", "wide", "tile", "staged32")
 
     def tuning(self, forward=True):
         """[(class, {last, sub, log2_n, log2_inner_bytes}, applicable kernel
@@ -188,7 +188,8 @@ class Batch:
         for c, k, x in zip(cl[:n.value], ks[:n.value], ch[:n.value]):
             desc = {"last": c & 1, "sub": (c >> 1) & 1,
                     "log2_n": (c >> 2) & 63, "log2_inner_bytes": c >> 8}
-            names = [self.KERNELS[i] for i in range(4) if (k >> i) & 1]
+            names = [self.KERNELS[i] for i in range(len(self.KERNELS))
+                     if (k >> i) & 1]
             out.append((c, desc, names, self.KERNELS[x]))
         return out
 

@@ -17,6 +17,10 @@
 
 namespace ddc {
 
+// DDC's coordinate types: element uids are unsigned, differences signed.
+using DiscreteElementType = std::size_t;
+using DiscreteVectorElement = std::ptrdiff_t;
+
 namespace detail {
 template <class T, class... Ts> constexpr std::size_t index_of() {
   constexpr bool same[] = {std::is_same_v<T, Ts>...};

@@ -6,6 +6,10 @@
 //   hierarchize / dehierarchize           (paliwa_transform.hpp:401-431)
 //   hierarchize_in<Dim> / dehierarchize_in<Dim>           (:346-399)
 //   transform_in<Dim> (full-grid overload)               (:215-251)
+//   transform_in<Dim> (restricted outputs)               (:258-344)
+//   for_each_transform_index<Dim>            (paliwa_domains.hpp:454-469)
+//   transform_bounds, covering_periodic_bounds, pole_pass_segments
+//                                  (paliwa_plan.hpp, paliwa_domains.hpp)
 //   strided_domain_from_level                (paliwa_domains.hpp:33-49)
 // Grids are ChunkSpans whose data_handle() is device memory holding the dense
 // row-major storage of strided_domain_from_level(level, maximum_level).
@@ -34,6 +38,7 @@
 #endif
 
 #include "../paliwa_gb300.h"
+#include "paliwa_plan.hpp"
 #include "paliwa_wavelets.hpp"
 
 namespace paliwa {
@@ -249,6 +254,74 @@ constexpr void dehierarchize(ChunkSpanType const strided_grid,
       static_cast<void *>(strided_grid.data_handle()), gb300::dtype_of<T>(),
       static_cast<int>(lv.size()), lv.data(), ln.data(), lm.data(),
       gb300::wavelet_id(wavelet_name), gb300::stream_of(instance)));
+}
+
+// paliwa_domains.hpp:454-469: visit every uid of per-level bounds (level 0:
+// multiples of the period; level h: odd points of level h).
+template <typename Dim, typename Visit>
+void for_each_transform_index(std::vector<PeriodicBounds> const &bounds,
+                              long maximum_level, Visit visit) {
+  long const period = 1L << maximum_level;
+  for (size_t h = 0; h < bounds.size(); ++h) {
+    auto const b = bounds[h];
+    if (b.empty()) continue;
+    long const stride = h == 0 ? period : 2L << (maximum_level - h);
+    long const last = b.max + (b.min > b.max ? period : 0);
+    for (long x = b.min; x <= last; x += stride)
+      visit(ddc::DiscreteElement<Dim>(std::array<long, 1>{x % period}));
+  }
+}
+
+// Restricted-output transform (paliwa_transform.hpp:333-344): the lifting
+// sequence along Dim, writing only what `outputs` depends on. The grid's
+// domain is a window of the level's lattice (strides 2^(L - l)) that holds
+// every required input; PoleExecution is accepted for source compatibility
+// (the device path plans its own work).
+template <class Dim, class ChunkSpanType, class LevelRange, class ExecSpace,
+          class... Dims>
+constexpr bool transform_in(
+    ChunkSpanType grid, ddc::DiscreteVector<Dims...> const &level,
+    ddc::DiscreteVector<Dims...> const &maximum_level,
+    LevelRange const &levels, LiftingPasses const &filters,
+    ddc::StridedDiscreteDomain<Dims...> const &outputs, ExecSpace instance,
+    PoleExecution = PoleExecution::Direct) {
+  using T = typename ChunkSpanType::element_type;
+  auto const lv = gb300::levels_of(level);
+  auto const lm = gb300::levels_of(maximum_level);
+  constexpr size_t n = sizeof...(Dims);
+  auto const dom = grid.domain();
+  std::array<int64_t, n> wf{}, we{}, of{}, oe{}, os{};
+  size_t i = 0;
+  ((wf[i] = static_cast<int64_t>(dom.front().template uid<Dims>()),
+    we[i] = static_cast<int64_t>(dom.extents().template get<Dims>()),
+    of[i] = static_cast<int64_t>(outputs.front().template uid<Dims>()),
+    oe[i] = static_cast<int64_t>(outputs.extents().template get<Dims>()),
+    os[i] = static_cast<int64_t>(outputs.strides().template get<Dims>()),
+    ++i),
+   ...);
+  i = 0;
+  ((static_cast<int64_t>(dom.strides().template get<Dims>()) ==
+            (int64_t{1} << (lm[i] - lv[i]))
+        ? void(++i)
+        : throw std::invalid_argument(
+              "the grid's strides must be the level's spacing")),
+   ...);
+  std::vector<int64_t> ls;
+  for (auto l : levels) ls.push_back(static_cast<int64_t>(l));
+  std::vector<int32_t> offs;
+  std::vector<double> co;
+  for (auto const &[o, f] : filters) {
+    offs.push_back(o);
+    co.insert(co.end(), f.begin(), f.end());
+  }
+  gb300::check(paliwa_gb_transform_outputs(
+      static_cast<void *>(grid.data_handle()), gb300::dtype_of<T>(),
+      static_cast<int>(n), lv.data(), lm.data(), wf.data(), we.data(),
+      gb300::dim_index<Dim, Dims...>(), ls.data(),
+      static_cast<int>(ls.size()), offs.data(), co.data(),
+      static_cast<int>(offs.size()), of.data(), oe.data(), os.data(),
+      gb300::stream_of(instance)));
+  return true;
 }
 
 } // namespace paliwa

@@ -115,6 +115,59 @@ int paliwa_gb_dehierarchize(void *grid, int dtype, int ndim,
                             const int64_t *maximum_level, int wavelet,
                             void *stream);
 
+/* ------------------------------------------------------------------------
+ * Restricted-output transform along one axis.
+ *
+ * Replaces paliwa::transform_bounds (paliwa/paliwa_domains.hpp:357-452):
+ * the exact access sets of the lifting sequence `levels` x passes (only the
+ * filter offsets matter) that make the output interval
+ * [outputs_min, outputs_max] (finest-level uids, min > max wraps, min < 0
+ * empty) exact. bounds receives 2 * (level + 1) values: the required input
+ * bounds (min, max) per hierarchical level 0..level, -1 -1 where empty.
+ * writes (optional, may be NULL) receives 2 * nlevels * nfilters values: the
+ * write bounds of each (level index, pass). Host-only: touches no GPU. */
+int paliwa_gb_transform_bounds(int64_t outputs_min, int64_t outputs_max,
+                               int64_t level, int64_t maximum_level,
+                               const int64_t *levels, int nlevels,
+                               const int32_t *offsets, int nfilters,
+                               int64_t *bounds, int64_t *writes);
+
+/* Replaces paliwa::transform_in(grid, level, maximum_level, levels, filters,
+ * outputs, exec, PoleExecution) (paliwa/paliwa_transform.hpp:333-344, via
+ * detail::transform_with_remote :258-331): the lifting sequence along `dim`
+ * restricted to the points that the outputs depend on. Leaves the buffer as
+ * the reference leaves its grid: outputs exact, the dependency cone holding
+ * the intermediate values, everything else untouched.
+ * The grid is a window buffer (F64 or F32): along dimension d it holds the
+ * uids (window_front[d] + k * 2^(L[d] - level[d])) mod 2^L[d] for
+ * k < window_extents[d], dense and row-major; the full grid is front 0,
+ * extents 2^level. Windows may wrap around the period, so one buffer can hold
+ * a slab and its periodic halo. outputs_* describe a strided domain in uids
+ * (front in [0, 2^L), extents, strides); along `dim` it sets the output
+ * interval, in the other dimensions the transformed columns, which must be
+ * grid points inside the window. Errors: PALIWA_GB_INVALID_ARGUMENT for
+ * shapes and levels (std::invalid_argument), PALIWA_GB_RUNTIME_ERROR when a
+ * required input lies outside the window ("Transform domain is missing
+ * required input values", :282-289). Empty outputs return at once. */
+int paliwa_gb_transform_outputs(
+    void *grid, int dtype, int ndim, const int64_t *level,
+    const int64_t *maximum_level, const int64_t *window_front,
+    const int64_t *window_extents, int dim, const int64_t *levels,
+    int nlevels, const int32_t *offsets, const double *coefficients,
+    int nfilters, const int64_t *outputs_front,
+    const int64_t *outputs_extents, const int64_t *outputs_strides,
+    void *stream);
+
+/* Replaces paliwa::dump_chunk_span_to_binary_file (paliwa/paliwa_io.hpp:13-23):
+ * writes `bytes` bytes of device memory at `data` (a grid's dense row-major
+ * storage) to `filename`, truncating it, in storage order with no header --
+ * the raw format paliwa/postprocess.py reads with numpy.fromfile. The copy is
+ * ordered after the work already queued on `stream`; the call returns once
+ * the file is written. PALIWA_GB_RUNTIME_ERROR if the file cannot be opened
+ * or written. */
+int paliwa_gb_dump_to_binary_file(const void *data, int64_t bytes,
+                                  const char *filename, void *stream);
+
 /* The transform of paliwa_gb_hierarchize (direction 1) or
  * paliwa_gb_dehierarchize (direction -1) without any device allocation.
  * No counterpart in the reference: it is for callers that cannot let a

@@ -19,7 +19,8 @@ from .transform import (dehierarchize, dehierarchize_in, hierarchize,
                         hierarchize_in,
                         lifting_wavelet_filter_offsets_and_coefficients,
                         lifting_wavelet_reconstruct_offsets_and_coefficients,
-                        transform_in, wavelet_id)
+                        transform_bounds, transform_in, transform_outputs,
+                        wavelet_id)
 
 __all__ = [
     "CudaError", "DeviceTimeout", "InvalidArgument", "OutOfRange",
@@ -30,6 +31,6 @@ __all__ = [
     "strided_hierarchical_domain_from_level", "dehierarchize",
     "dehierarchize_in", "hierarchize", "hierarchize_in",
     "lifting_wavelet_filter_offsets_and_coefficients",
-    "lifting_wavelet_reconstruct_offsets_and_coefficients", "transform_in",
-    "wavelet_id",
+    "lifting_wavelet_reconstruct_offsets_and_coefficients", "transform_bounds",
+    "transform_in", "transform_outputs", "wavelet_id",
 ]

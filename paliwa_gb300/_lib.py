@@ -45,6 +45,14 @@ SIGNATURES = {
         _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _i, _vp]),
     "paliwa_gb_hierarchize": (_i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _vp]),
     "paliwa_gb_dehierarchize": (_i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _vp]),
+    "paliwa_gb_transform_bounds": (
+        _i, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+             _pi64, _i, _pi32, _i, _pi64, _pi64]),
+    "paliwa_gb_transform_outputs": (
+        _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _pi64, _i, _pi64, _i, _pi32,
+             _pd, _i, _pi64, _pi64, _pi64, _vp]),
+    "paliwa_gb_dump_to_binary_file": (
+        _i, [_vp, ctypes.c_int64, ctypes.c_char_p, _vp]),
     "paliwa_gb_transform_noalloc": (
         _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _i, _vp]),
     "paliwa_gb_batch_create": (

@@ -155,3 +155,70 @@ def transform_in(grid, dim, level, maximum_level, levels, filters,
            _lib.f64([c for _, f in filters for c in f]), len(filters)),
           stream)
     return True
+
+
+def transform_bounds(outputs, level, maximum_level, levels, filters):
+    """paliwa::transform_bounds (paliwa_domains.hpp:357-452) through the
+    library's host planner: ``outputs`` is ``None`` (empty) or ``(min, max)``
+    in finest-level uids (min > max wraps). Returns ``(bounds, writes)``:
+    the required input bounds per hierarchical level 0..level and the write
+    bounds of each (level index, pass), each ``None`` or ``(min, max)``.
+    Only the filter offsets are read. Host code; needs no GPU."""
+    import ctypes
+    levels = [int(l) for l in levels]
+    filters = list(filters)
+    lo, hi = (-1, -1) if outputs is None else (int(outputs[0]),
+                                               int(outputs[1]))
+    nb = 2 * (int(level) + 1)
+    nw = 2 * max(1, len(levels) * len(filters))
+    b = (ctypes.c_int64 * nb)()
+    w = (ctypes.c_int64 * nw)()
+    _lib.check(_lib.load().paliwa_gb_transform_bounds(
+        lo, hi, int(level), int(maximum_level), _lib.i64(levels), len(levels),
+        _lib.i32([o for o, _ in filters]), len(filters), b, w))
+
+    def pairs(a, n):
+        return [None if a[2 * k] < 0 else (a[2 * k], a[2 * k + 1])
+                for k in range(n)]
+
+    bounds = pairs(b, int(level) + 1)
+    flat = pairs(w, len(levels) * len(filters))
+    writes = [flat[i * len(filters):(i + 1) * len(filters)]
+              for i in range(len(levels))]
+    return bounds, writes
+
+
+def transform_outputs(grid, dim, level, maximum_level, levels, filters,
+                      outputs, window_front=None, stream=None):
+    """transform_in<Dim>(grid, level, maximum_level, levels, filters,
+    outputs, ...) (paliwa_transform.hpp:258-344): the lifting sequence along
+    ``dim`` restricted to the points the outputs depend on.
+
+    ``grid`` is a C-contiguous float64 or float32 CUDA tensor holding a
+    window of the grid: along dimension d its ``grid.shape[d]`` points are
+    the uids ``(window_front[d] + k * 2^(L[d] - level[d])) mod 2^L[d]``
+    (default front 0; the full grid is front 0 with 2^level points).
+    ``outputs`` is ``(front, extents, strides)`` in uids, like a
+    ``StridedDiscreteDomain``. A required input outside the window raises
+    PaliwaError (the reference's std::runtime_error)."""
+    import torch
+    if not isinstance(grid, torch.Tensor) or not grid.is_cuda:
+        raise _lib.InvalidArgument("grid must be a CUDA tensor")
+    if not grid.is_contiguous():
+        raise _lib.InvalidArgument("grid must be C-contiguous")
+    nd = len(level)
+    if grid.dim() != nd:
+        raise _lib.InvalidArgument("grid must have one axis per dimension")
+    if window_front is None:
+        window_front = (0,) * nd
+    front, extents, strides = outputs
+    filters = list(filters)
+    levels = [int(l) for l in levels]
+    _call("paliwa_gb_transform_outputs", grid,
+          (_dtype_code(grid, False), nd, _lib.i64(level),
+           _lib.i64(maximum_level), _lib.i64(window_front),
+           _lib.i64(grid.shape), int(dim), _lib.i64(levels), len(levels),
+           _lib.i32([o for o, _ in filters]),
+           _lib.f64([c for _, f in filters for c in f]), len(filters),
+           _lib.i64(front), _lib.i64(extents), _lib.i64(strides)), stream)
+    return True

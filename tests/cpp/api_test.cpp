@@ -7,10 +7,12 @@
 
 #include <cmath>
 #include <cstdio>
+#include <limits>
 #include <random>
 #include <stdexcept>
 #include <vector>
 
+#include <paliwa/paliwa_io.hpp>
 #include <paliwa/paliwa_transform.hpp>
 
 #include "paliwa_oracle.hpp"
@@ -59,6 +61,49 @@ int main() {
   ddc::ChunkSpan<double, Dom> partial(reinterpret_cast<double *>(256), part);
   EXPECT(throws<std::invalid_argument>(
       [&] { paliwa::hierarchize(partial, level, lmin, lmax, "hat"); }));
+
+  // Restricted-output planning (paliwa_domains.hpp), host only: the
+  // reference's known answers (test/test_paliwa_plan.cpp:199-221, 403-429).
+  {
+    paliwa::LiftingPasses const one{{1, {0.0, 1.0, 0.0}}};
+    auto ignore = [](size_t, size_t, paliwa::PeriodicBounds) {};
+    for (auto const &ls : std::vector<std::vector<long>>{{4, 1}, {1, 4}, {1, 2, 1}})
+      EXPECT(throws<std::invalid_argument>(
+          [&] { paliwa::transform_bounds({0, 0}, 4, 4, ls, one, ignore); }));
+    auto cover = [](std::vector<long> v, long lo, long hi) {
+      auto b = paliwa::covering_periodic_bounds(v, 64);
+      return b.min == lo && b.max == hi;
+    };
+    EXPECT(cover({}, -1, -1) && cover({12}, 12, 12) &&
+           cover({8, 12, 16}, 8, 16) && cover({0, 4, 56, 60}, 56, 4) &&
+           cover({0, 16, 32, 48}, 0, 48));
+    constexpr int big = std::numeric_limits<std::ptrdiff_t>::digits;
+    std::size_t const sp = std::size_t{1} << (big - 3);
+    auto runs = paliwa::pole_pass_segments(
+        {static_cast<long>(sp), static_cast<long>(5 * sp)}, 6 * sp, 3, big, 3);
+    std::vector<std::array<int, 3>> got;
+    for (auto const &r : runs)
+      for (int k = 0; k < r.count; ++k)
+        got.push_back({r.first + k * r.stride, r.lower + k * r.stride,
+                       r.upper + k * r.stride});
+    EXPECT((got == std::vector<std::array<int, 3>>{{3, 2, 4}, {5, 4, 6}, {7, 6, 0}}));
+    EXPECT(throws<std::invalid_argument>([] {
+      paliwa::pole_pass_segments({0, 0}, 0, std::numeric_limits<int>::digits,
+                                 std::numeric_limits<int>::digits, 1);
+    }));
+    // A window holding uids 0..7 of a 16-point axis cannot give outputs
+    // 4..7 of the full hierarchization: their inputs wrap to 8..15.
+    using V1 = ddc::DiscreteVector<X>;
+    using D1 = ddc::StridedDiscreteDomain<X>;
+    D1 const win(ddc::DiscreteElement<X>(std::array<long, 1>{0}), V1(8), V1(1));
+    D1 const outs(ddc::DiscreteElement<X>(std::array<long, 1>{4}), V1(4), V1(1));
+    ddc::ChunkSpan<double, D1> w(reinterpret_cast<double *>(256), win);
+    EXPECT(throws<std::runtime_error>([&] {
+      paliwa::transform_in<X>(w, V1(4), V1(4), std::vector<long>{4, 3, 2, 1},
+                              paliwa::LiftingPasses{{1, {-0.5, 1.0, -0.5}}},
+                              outs, paliwa::gb300::Stream{});
+    }));
+  }
 
   int devices = 0;
   if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0) {
@@ -117,6 +162,42 @@ int main() {
                             paliwa::LiftingPasses{{2, {0.0, 1.0, 0.0}}},
                             instance);
   }));
+  // Restricted outputs covering the whole grid equal the full transform_in.
+  {
+    std::vector<double> full(host.size()), part(host.size());
+    std::vector<long> ls{3, 2, 1};
+    auto const &f = paliwa::lifting_wavelet_filter_offsets_and_coefficients
+                        .at("biorthogonal");
+    EXPECT(cudaMemcpy(dev, host.data(), host.size() * sizeof(double),
+                      cudaMemcpyHostToDevice) == cudaSuccess);
+    paliwa::transform_in<Y>(grid, level, lmax, ls, f, instance);
+    EXPECT(cudaStreamSynchronize(s) == cudaSuccess);
+    EXPECT(cudaMemcpy(full.data(), dev, full.size() * sizeof(double),
+                      cudaMemcpyDeviceToHost) == cudaSuccess);
+    EXPECT(cudaMemcpy(dev, host.data(), host.size() * sizeof(double),
+                      cudaMemcpyHostToDevice) == cudaSuccess);
+    paliwa::transform_in<Y>(grid, level, lmax, ls, f, dom, instance,
+                            paliwa::PoleExecution::PackedPoles);
+    EXPECT(cudaStreamSynchronize(s) == cudaSuccess);
+    EXPECT(cudaMemcpy(part.data(), dev, part.size() * sizeof(double),
+                      cudaMemcpyDeviceToHost) == cudaSuccess);
+    EXPECT(part == full);
+  }
+  // Raw dump (paliwa_io.hpp): storage order, no header.
+  {
+    char const *path = "api_test_dump.raw";
+    paliwa::dump_chunk_span_to_binary_file(grid, path, instance);
+    std::vector<double> back(host.size()), now(host.size());
+    std::FILE *f = std::fopen(path, "rb");
+    EXPECT(f != nullptr);
+    EXPECT(std::fread(back.data(), sizeof(double), back.size(), f) ==
+           back.size());
+    std::fclose(f);
+    std::remove(path);
+    EXPECT(cudaMemcpy(now.data(), dev, now.size() * sizeof(double),
+                      cudaMemcpyDeviceToHost) == cudaSuccess);
+    EXPECT(back == now);
+  }
   cudaStreamDestroy(s);
   cudaFree(dev);
   std::printf("api_test: GPU transforms match the oracle\n");

@@ -314,7 +314,8 @@ def run_reference(args, w, world, rank):
 DRAM_RATIO_FILE = "profiles/lift_kernels_4d_ct_20_dram_ratio.txt"
 # Groups of grids whose host copies overlap each other's transforms in the
 # end-to-end measurement.
-E2E_GROUPS = 8
+E2E_GROUPS = 16
+E2E_COPY_STREAMS = 1
 
 
 def dram_ratio(kernel):
@@ -560,7 +561,8 @@ def run_gpu(args, w, world, rank, local):
     bt64.close()
     del b64, v64
     hb = pct.HostBatch(w.levels, w.lmin, w.lmax, w.wavelet, torch.float32,
-                       compensated=True, groups=E2E_GROUPS, device=dev)
+                       compensated=True, groups=E2E_GROUPS, device=dev,
+                       batch_groups=1, copy_streams=E2E_COPY_STREAMS)
     host_in = torch.empty(hb.numel(), dtype=torch.float32).pin_memory()
     host_in.copy_(b32)
     host_out = torch.empty_like(host_in).pin_memory()

@@ -211,6 +211,15 @@ int paliwa_gb_batch_hierarchize(paliwa_gb_batch *batch, void *stream);
 int paliwa_gb_batch_dehierarchize(paliwa_gb_batch *batch, void *stream);
 /* enable != 0 (default): capture and replay CUDA graphs. */
 int paliwa_gb_batch_use_graphs(paliwa_gb_batch *batch, int enable);
+/* Splits the batch into `ngroups` groups of about equal size (grids dealt
+ * largest first), each planned on its own and run on its own branch (forked
+ * streams, joined into the caller's stream), so that the groups' launches
+ * overlap; creation uses 4 (fewer when there are fewer grids). 1 runs every
+ * launch on the caller's stream. Re-plans both directions (the autotuner's
+ * choices are kept) after synchronizing the device. No counterpart in the
+ * reference (its CT driver spreads grids over execution-space instances,
+ * test/test_paliwa_combination_technique.cpp:164-174). */
+int paliwa_gb_batch_set_groups(paliwa_gb_batch *batch, int ngroups);
 int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
                          int64_t *launches_forward,
                          int64_t *launches_inverse);

@@ -61,6 +61,7 @@ SIGNATURES = {
     "paliwa_gb_batch_hierarchize": (_i, [_vp, _vp]),
     "paliwa_gb_batch_dehierarchize": (_i, [_vp, _vp]),
     "paliwa_gb_batch_use_graphs": (_i, [_vp, _i]),
+    "paliwa_gb_batch_set_groups": (_i, [_vp, _i]),
     "paliwa_gb_batch_info": (_i, [_vp, _pi64, _pi64, _pi64]),
     "paliwa_gb_batch_profile": (
         _i, [_vp, _i, _vp, _i, ctypes.POINTER(_i),

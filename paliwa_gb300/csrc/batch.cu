@@ -6,9 +6,14 @@
 // (test/test_paliwa_combination_technique.cpp:164-174). Here one plan covers
 // every grid: for each axis, the per-grid stages of plan_axis() are merged
 // into one launch per stage index and chunk size, whose device-side job list
-// names every grid. The launch sequence of a direction is captured once into
-// a CUDA graph and replayed.
+// names every grid. The grids are dealt into up to kBatchGroups groups of
+// about equal size, each planned on its own; a direction's launch sequences
+// of the groups run on parallel branches (forked streams, joined at the
+// end), so one group's launches fill the tails of another's and kernels of
+// different kinds share the GPU. The whole direction is captured once into a
+// CUDA graph and replayed.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -24,7 +29,13 @@ using namespace pgb;
 
 namespace {
 
+// Groups of grids planned and run on parallel branches. Measured on the 4D
+// CT workload (3,025 grids, FP32c, forward + inverse): 28.7 ms with one
+// group, 26.1 with two, 25.7 with three, 25.6 with four.
+constexpr int kBatchGroups = 4;
+
 struct Launch {
+  int group = 0;
   int R = 0;
   int sched = -1;
   size_t job_first = 0;  // index into the device job array
@@ -97,9 +108,18 @@ struct paliwa_gb_batch {
   std::vector<int64_t> levels, lmin;
   std::vector<void *> grids;
   // Shadow buffers of the windowed stages (grids with pencils longer than
-  // one CTA holds), reused by every axis: one direction runs at a time.
+  // one CTA holds), reused by every axis of a group (a group's axes run in
+  // order); the groups, which run concurrently, have disjoint regions.
   void *shadow = nullptr;
   size_t shadow_bytes = 0;
+  // group[g]: the group of grid g; group_shadow[k]: byte offset of group
+  // k's shadow region. Group k > 0 runs on streams[k - 1] (non-blocking),
+  // forked from and joined into the caller's stream with events.
+  int ngroups = 1;
+  std::vector<int> group;
+  std::vector<size_t> group_shadow;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;  // [0] fork, [k] join of group k
 };
 
 namespace {
@@ -113,62 +133,72 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
   dr.symmetric = symmetric_filters(filters);
   std::vector<LiftJob> all_jobs;
   size_t const es = dtype_size(b.dtype);
-  for (int d = 0; d < b.ndim; ++d) {
-    // stages[g] = the ordered stages of grid g along axis d
-    std::vector<std::vector<Stage>> stages(b.ngrids);
-    size_t depth = 0;
-    size_t shadow_off = 0;
-    for (int g = 0; g < b.ngrids; ++g) {
-      int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
-      AxisView view =
-          axis_view(reinterpret_cast<unsigned long long>(grid_ptrs[g]),
-                    b.ndim, lv, d, b.dtype);
-      auto const shifts = level_shifts(lv[d], lmin[d], forward);
-      if (needs_shadow(view, shifts)) {
-        size_t bytes = es;
-        for (int k = 0; k < b.ndim; ++k) bytes <<= lv[k];
-        if (shadow_off + bytes > b.shadow_bytes)
-          throw StatusError(PALIWA_GB_RUNTIME_ERROR, "shadow plan overflow");
-        view.shadow =
-            reinterpret_cast<unsigned long long>(b.shadow) + shadow_off;
-        shadow_off += (bytes + 255) / 256 * 256;
-      }
-      plan_axis(view, shifts, filters, stages[g], &dr.tuning);
-      for (Stage const &st : stages[g]) {
-        if (st.kernels == 0) continue;
-        auto &ci = dr.classes[st.tclass];
-        if (ci.kernels == 0) {
-          ci.kernels = st.kernels;
-          ci.dflt = st.dflt;
+  for (int grp = 0; grp < b.ngroups; ++grp) {
+    std::vector<int> members;
+    for (int g = 0; g < b.ngrids; ++g)
+      if (b.group[g] == grp) members.push_back(g);
+    for (int d = 0; d < b.ndim; ++d) {
+      // stages[i] = the ordered stages of grid members[i] along axis d
+      std::vector<std::vector<Stage>> stages(members.size());
+      size_t depth = 0;
+      size_t shadow_off = b.group_shadow[grp];
+      for (size_t i = 0; i < members.size(); ++i) {
+        int const g = members[i];
+        int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
+        AxisView view =
+            axis_view(reinterpret_cast<unsigned long long>(grid_ptrs[g]),
+                      b.ndim, lv, d, b.dtype);
+        auto const shifts = level_shifts(lv[d], lmin[d], forward);
+        if (needs_shadow(view, shifts)) {
+          size_t bytes = es;
+          for (int k = 0; k < b.ndim; ++k) bytes <<= lv[k];
+          if (shadow_off + bytes > b.shadow_bytes)
+            throw StatusError(PALIWA_GB_RUNTIME_ERROR,
+                              "shadow plan overflow");
+          view.shadow =
+              reinterpret_cast<unsigned long long>(b.shadow) + shadow_off;
+          shadow_off += (bytes + 255) / 256 * 256;
         }
-        ci.points += st.job.columns << st.job.log2_n;
-      }
-      depth = std::max(depth, stages[g].size());
-    }
-    for (size_t k = 0; k < depth; ++k) {
-      // One launch per chunk size among the k-th stages of every grid.
-      std::map<int, std::vector<Stage const *>> by_r;
-      for (int g = 0; g < b.ngrids; ++g)
-        if (k < stages[g].size()) by_r[stages[g][k].R].push_back(&stages[g][k]);
-      for (auto const &[R, list] : by_r) {
-        Launch L;
-        L.R = R;
-        int const ws = wavelet_schedule(filters);
-        L.sched = ws;
-        for (Stage const *st : list)
-          if (ws < 0 || !canonical_shifts(st->job, (ws & 1) != 0)) L.sched = -1;
-        L.job_first = all_jobs.size();
-        L.njobs = static_cast<int>(list.size());
-        for (Stage const *st : list) {
-          LiftJob job = st->job;
-          job.tile_begin = L.tiles;
-          L.tiles += st->tiles;
-          L.points += st->R == kCopy
-                          ? st->job.columns / static_cast<long long>(es)
-                          : st->job.columns << st->job.log2_n;
-          all_jobs.push_back(job);
+        plan_axis(view, shifts, filters, stages[i], &dr.tuning);
+        for (Stage const &st : stages[i]) {
+          if (st.kernels == 0) continue;
+          auto &ci = dr.classes[st.tclass];
+          if (ci.kernels == 0) {
+            ci.kernels = st.kernels;
+            ci.dflt = st.dflt;
+          }
+          ci.points += st.job.columns << st.job.log2_n;
         }
-        if (L.R != 0 && L.tiles > 0) dr.launches.push_back(L);
+        depth = std::max(depth, stages[i].size());
+      }
+      for (size_t k = 0; k < depth; ++k) {
+        // One launch per chunk size among the k-th stages of the group.
+        std::map<int, std::vector<Stage const *>> by_r;
+        for (size_t i = 0; i < members.size(); ++i)
+          if (k < stages[i].size())
+            by_r[stages[i][k].R].push_back(&stages[i][k]);
+        for (auto const &[R, list] : by_r) {
+          Launch L;
+          L.group = grp;
+          L.R = R;
+          int const ws = wavelet_schedule(filters);
+          L.sched = ws;
+          for (Stage const *st : list)
+            if (ws < 0 || !canonical_shifts(st->job, (ws & 1) != 0))
+              L.sched = -1;
+          L.job_first = all_jobs.size();
+          L.njobs = static_cast<int>(list.size());
+          for (Stage const *st : list) {
+            LiftJob job = st->job;
+            job.tile_begin = L.tiles;
+            L.tiles += st->tiles;
+            L.points += st->R == kCopy
+                            ? st->job.columns / static_cast<long long>(es)
+                            : st->job.columns << st->job.log2_n;
+            all_jobs.push_back(job);
+          }
+          if (L.R != 0 && L.tiles > 0) dr.launches.push_back(L);
+        }
       }
     }
   }
@@ -182,16 +212,30 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
 }
 
 void run_direction(paliwa_gb_batch &b, Direction &dr, cudaStream_t s) {
+  // Group 0 runs on the caller's stream, group k > 0 on streams[k - 1],
+  // forked after the work already queued on `s` and joined back into it.
   auto launch_all = [&] {
+    if (b.ngroups > 1)
+      cuda_check(cudaEventRecord(b.events[0], s), "cudaEventRecord(fork)");
+    for (int k = 1; k < b.ngroups; ++k)
+      cuda_check(cudaStreamWaitEvent(b.streams[k - 1], b.events[0], 0),
+                 "cudaStreamWaitEvent(fork)");
     for (auto const &L : dr.launches)
       launch_lift(b.dtype, dr.exact, dr.symmetric, L.sched, L.R, dr.params,
-                  dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
+                  dr.jobs_dev + L.job_first, L.njobs, L.tiles,
+                  L.group == 0 ? s : b.streams[L.group - 1]);
+    for (int k = 1; k < b.ngroups; ++k) {
+      cuda_check(cudaEventRecord(b.events[k], b.streams[k - 1]),
+                 "cudaEventRecord(join)");
+      cuda_check(cudaStreamWaitEvent(s, b.events[k], 0),
+                 "cudaStreamWaitEvent(join)");
+    }
   };
   cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
   if (s != nullptr)
     cuda_check(cudaStreamIsCapturing(s, &status), "cudaStreamIsCapturing");
   // The legacy default stream cannot be captured; a stream that is already
-  // capturing records our launches into the caller's graph.
+  // capturing records our launches (and the fork) into the caller's graph.
   if (!b.use_graphs || s == nullptr || status != cudaStreamCaptureStatusNone) {
     launch_all();
     return;
@@ -215,6 +259,80 @@ void run_direction(paliwa_gb_batch &b, Direction &dr, cudaStream_t s) {
   cuda_check(cudaGraphLaunch(dr.graph, s), "cudaGraphLaunch");
 }
 
+// Deals the grids, largest first, round-robin into groups, and sizes each
+// group's shadow region (the largest per-axis total over the group's grids
+// whose pencils along that axis need windowed stages).
+void assign_groups(paliwa_gb_batch &b, int64_t const *levels,
+                   int64_t const *lmin, int want) {
+  size_t const es = dtype_size(b.dtype);
+  std::vector<int> order(b.ngrids);
+  std::vector<int> log2size(b.ngrids, 0);
+  for (int g = 0; g < b.ngrids; ++g) {
+    order[g] = g;
+    for (int d = 0; d < b.ndim; ++d)
+      log2size[g] += static_cast<int>(levels[g * b.ndim + d]);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+    return log2size[a] > log2size[c];
+  });
+  b.ngroups = std::max(1, std::min(want, b.ngrids));
+  b.group.assign(b.ngrids, 0);
+  for (int i = 0; i < b.ngrids; ++i) b.group[order[i]] = i % b.ngroups;
+  b.group_shadow.assign(b.ngroups, 0);
+  b.shadow_bytes = 0;
+  for (int k = 0; k < b.ngroups; ++k) {
+    size_t need = 0;
+    for (int d = 0; d < b.ndim; ++d) {
+      size_t total = 0;
+      for (int g = 0; g < b.ngrids; ++g) {
+        if (b.group[g] != k) continue;
+        int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
+        if (lv[d] <= kWindowLog2 || lv[d] == lmin[d]) continue;
+        size_t bytes = es;
+        for (int j = 0; j < b.ndim; ++j) bytes <<= lv[j];
+        total += (bytes + 255) / 256 * 256;
+      }
+      need = std::max(need, total);
+    }
+    b.group_shadow[k] = b.shadow_bytes;
+    b.shadow_bytes += need;
+  }
+}
+
+void free_batch_streams(paliwa_gb_batch &b) {
+  for (cudaStream_t st : b.streams)
+    if (st != nullptr) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : b.events)
+    if (ev != nullptr) cudaEventDestroy(ev);
+  b.streams.clear();
+  b.events.clear();
+}
+
+// (Re)groups the batch into `want` groups and plans both directions (keeping
+// the autotuner's choices): shadow regions, branch streams and events.
+void setup_groups(paliwa_gb_batch &b, int want) {
+  free_direction(b.dir[0]);
+  free_direction(b.dir[1]);
+  free_batch_streams(b);
+  if (b.shadow) cudaFree(b.shadow);
+  b.shadow = nullptr;
+  assign_groups(b, b.levels.data(), b.lmin.data(), want);
+  if (b.shadow_bytes)
+    cuda_check(cudaMalloc(&b.shadow, b.shadow_bytes), "cudaMalloc(shadow)");
+  b.events.assign(b.ngroups, nullptr);
+  for (auto &ev : b.events)
+    cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming),
+               "cudaEventCreate");
+  b.streams.assign(b.ngroups - 1, nullptr);
+  for (auto &st : b.streams)
+    cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking),
+               "cudaStreamCreate");
+  plan_direction(b, b.dir[0], true, b.levels.data(), b.lmin.data(),
+                 b.grids.data());
+  plan_direction(b, b.dir[1], false, b.levels.data(), b.lmin.data(),
+                 b.grids.data());
+}
+
 } // namespace
 
 // ---------------------------------------------------------------------------
@@ -230,6 +348,8 @@ struct paliwa_gb_ct {
   CtSubspace *subspaces_dev = nullptr;
   int *lists_dev = nullptr;
   CtGrid *grids_dev = nullptr;
+  int *heavy_dev = nullptr;
+  long long *heavy_first_dev = nullptr;
   CtParams params{};
 };
 
@@ -320,9 +440,22 @@ void build_ct(paliwa_gb_ct &ct, int64_t const *levels,
     cuda_check(cudaMemcpy(*dst, v.data(), bytes, cudaMemcpyHostToDevice),
                what);
   };
+  std::vector<int> heavy;
+  std::vector<long long> heavy_first;
+  long long nheavy_points = 0;
+  for (size_t i = 0; i < subs.size(); ++i) {
+    if (subs[i].grid_end - subs[i].grid_begin <= kCtHeavy) continue;
+    heavy.push_back(static_cast<int>(i));
+    heavy_first.push_back(nheavy_points);
+    long long const next =
+        i + 1 < subs.size() ? subs[i + 1].offset : off;
+    nheavy_points += next - subs[i].offset;
+  }
   upload(&ct.subspaces_dev, subs, "upload subspaces");
   upload(&ct.lists_dev, lists, "upload grid lists");
   upload(&ct.grids_dev, grids, "upload grids");
+  upload(&ct.heavy_dev, heavy, "upload heavy subspaces");
+  upload(&ct.heavy_first_dev, heavy_first, "upload heavy offsets");
   std::memset(&ct.params, 0, sizeof(ct.params));
   ct.params.subspaces = ct.subspaces_dev;
   ct.params.nsubspaces = static_cast<int>(subs.size());
@@ -332,6 +465,38 @@ void build_ct(paliwa_gb_ct &ct, int64_t const *levels,
   ct.params.npoints = ct.npoints;
   for (int d = 0; d < nd && d < kMaxDims; ++d)
     ct.params.max_level[d] = static_cast<signed char>(lmax[d]);
+  ct.params.heavy = ct.heavy_dev;
+  ct.params.heavy_first = ct.heavy_first_dev;
+  ct.params.nheavy = static_cast<int>(heavy.size());
+  ct.params.nheavy_points = nheavy_points;
+  // Products c * v are exact in FP64 when c has at most 53 - 24 = 29
+  // significant bits and v is a float (whose magnitude lies in
+  // [2^-149, 2^128]), provided |c| stays within [2^-500, 2^500] so that the
+  // product neither underflows nor overflows. For FP64 grids only |c| = 1
+  // is exact for every value.
+  bool exact = true;
+  for (int g = 0; g < ct.ngrids && exact; ++g) {
+    double const c = coefficients[g];
+    if (c == 0.0) continue;
+    if (!std::isfinite(c)) {
+      exact = false;
+      break;
+    }
+    if (ct.dtype == PALIWA_GB_F64) {
+      exact = std::fabs(c) == 1.0;
+      continue;
+    }
+    int e = 0;
+    double m = std::frexp(std::fabs(c), &e);  // m in [0.5, 1)
+    long long bits = static_cast<long long>(std::ldexp(m, 53));
+    int sig = 53;
+    while ((bits & 1) == 0) {
+      bits >>= 1;
+      --sig;
+    }
+    if (sig > 29 || e < -500 || e > 500) exact = false;
+  }
+  ct.params.exact_products = exact ? 1 : 0;
 }
 
 template <int OP>
@@ -349,6 +514,15 @@ void ct_launch(paliwa_gb_ct const &ct, double *sparse, double *full,
   default: throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
   }
   cuda_check(cudaGetLastError(), "ct_kernel launch");
+  if (OP == kRestrict && p.nheavy_points > 0) {
+    unsigned const hblocks =
+        static_cast<unsigned>((p.nheavy_points * 32 + 255) / 256);
+    if (ct.dtype == PALIWA_GB_F64)
+      ct_heavy_restrict_kernel<double><<<hblocks, 256, 0, s>>>(p);
+    else
+      ct_heavy_restrict_kernel<float><<<hblocks, 256, 0, s>>>(p);
+    cuda_check(cudaGetLastError(), "ct_heavy_restrict_kernel launch");
+  }
 }
 
 } // namespace
@@ -385,28 +559,12 @@ int paliwa_gb_batch_create(int ndim, int ngrids, const int64_t *levels,
       for (int d = 0; d < ndim; ++d) total += levels[g * ndim + d];
       b->points += 1LL << total;
     }
-    // Shadow space: the largest per-axis total over the grids whose pencils
-    // along that axis need windowed stages.
-    for (int d = 0; d < ndim; ++d) {
-      size_t total = 0;
-      for (int g = 0; g < ngrids; ++g) {
-        int64_t const *lv = levels + static_cast<size_t>(g) * ndim;
-        if (lv[d] <= kWindowLog2 || lv[d] == minimum_level[d]) continue;
-        size_t bytes = es;
-        for (int k = 0; k < ndim; ++k) bytes <<= lv[k];
-        total += (bytes + 255) / 256 * 256;
-      }
-      b->shadow_bytes = std::max(b->shadow_bytes, total);
-    }
     try {
-      if (b->shadow_bytes)
-        cuda_check(cudaMalloc(&b->shadow, b->shadow_bytes),
-                   "cudaMalloc(shadow)");
-      plan_direction(*b, b->dir[0], true, levels, minimum_level, grid_ptrs);
-      plan_direction(*b, b->dir[1], false, levels, minimum_level, grid_ptrs);
+      setup_groups(*b, kBatchGroups);
     } catch (...) {
       free_direction(b->dir[0]);
       free_direction(b->dir[1]);
+      free_batch_streams(*b);
       if (b->shadow) cudaFree(b->shadow);
       throw;
     }
@@ -435,6 +593,17 @@ int paliwa_gb_batch_use_graphs(paliwa_gb_batch *batch, int enable) {
     if (batch == nullptr)
       throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
     batch->use_graphs = enable != 0;
+  });
+}
+
+int paliwa_gb_batch_set_groups(paliwa_gb_batch *batch, int ngroups) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    if (ngroups < 1)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "ngroups must be >= 1");
+    cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    setup_groups(*batch, ngroups);
   });
 }
 
@@ -599,6 +768,7 @@ void paliwa_gb_batch_destroy(paliwa_gb_batch *batch) {
   if (batch == nullptr) return;
   free_direction(batch->dir[0]);
   free_direction(batch->dir[1]);
+  free_batch_streams(*batch);
   if (batch->shadow) cudaFree(batch->shadow);
   delete batch;
 }
@@ -630,6 +800,8 @@ int paliwa_gb_ct_create(int ndim, int ngrids, const int64_t *levels,
       cudaFree(ct->subspaces_dev);
       cudaFree(ct->lists_dev);
       cudaFree(ct->grids_dev);
+      cudaFree(ct->heavy_dev);
+      cudaFree(ct->heavy_first_dev);
       throw;
     }
     *out = ct.release();
@@ -702,6 +874,8 @@ void paliwa_gb_ct_destroy(paliwa_gb_ct *ct) {
   cudaFree(ct->subspaces_dev);
   cudaFree(ct->lists_dev);
   cudaFree(ct->grids_dev);
+  cudaFree(ct->heavy_dev);
+  cudaFree(ct->heavy_first_dev);
   delete ct;
 }
 

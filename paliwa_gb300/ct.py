@@ -109,10 +109,12 @@ class Batch:
 
     ``grids`` are CUDA tensors (bound by address at construction),
     ``levels[i]`` the level vector of grid i; ``minimum_level`` and
-    ``maximum_level`` are shared, as in the reference's driver."""
+    ``maximum_level`` are shared, as in the reference's driver. ``groups``
+    (default: the library's, 4) is the number of groups of grids run on
+    parallel branches (see :meth:`set_groups`)."""
 
     def __init__(self, grids, levels, minimum_level, maximum_level,
-                 wavelet_name="hat", compensated=False):
+                 wavelet_name="hat", compensated=False, groups=None):
         _check_grids(grids, levels)
         self.grids = list(grids)
         self.levels = [tuple(int(x) for x in l) for l in levels]
@@ -126,6 +128,16 @@ class Batch:
             wavelet_id(wavelet_name), _ptr_array(grids),
             ctypes.byref(self._h)))
         self.points = sum(g.numel() for g in grids)
+        if groups is not None:
+            self.set_groups(groups)
+
+    def set_groups(self, ngroups):
+        """Split the grids into ``ngroups`` groups of about equal size, each
+        planned on its own and run on its own branch (forked from and joined
+        into the caller's stream) so that their launches overlap; 1 runs
+        every launch on the caller's stream. Synchronizes the device."""
+        _lib.check(self._lib.paliwa_gb_batch_set_groups(self._h,
+                                                        int(ngroups)))
 
     def hierarchize(self, stream=None):
         _lib.check(self._lib.paliwa_gb_batch_hierarchize(
@@ -235,11 +247,14 @@ class HostBatch:
     copies it out on a second copy stream once transformed, so that group
     g + 1 arrives and group g - 1 leaves while group g is transformed. Host
     buffers should be pinned (``pin_memory()``) for the copies to be
-    asynchronous."""
+    asynchronous. ``batch_groups`` is passed to every group's
+    :class:`Batch` (its parallel branches); ``copy_streams`` streams per
+    direction carry the copies (groups dealt round-robin), so that copies
+    of neighbouring groups in one direction may run at once."""
 
     def __init__(self, levels, minimum_level, maximum_level,
                  wavelet_name="hat", dtype=None, compensated=False, groups=8,
-                 device=None, align=64):
+                 device=None, align=64, batch_groups=None, copy_streams=1):
         import torch
         dtype = torch.float32 if dtype is None else dtype
         self.levels = [tuple(int(x) for x in l) for l in levels]
@@ -254,9 +269,14 @@ class HostBatch:
         self.spans = [(starts[a], ends[b - 1]) for a, b in self.ranges]
         self.batches = [Batch(self.grids[a:b], self.levels[a:b],
                               minimum_level, maximum_level, wavelet_name,
-                              compensated) for a, b in self.ranges]
+                              compensated, batch_groups)
+                        for a, b in self.ranges]
         dev = self.buf.device
-        self._streams = [torch.cuda.Stream(dev) for _ in range(3)]
+        k = max(1, int(copy_streams))
+        self._in = [torch.cuda.Stream(dev) for _ in range(k)]
+        self._out = [torch.cuda.Stream(dev) for _ in range(k)]
+        self._run = torch.cuda.Stream(dev)
+        self._streams = self._in + [self._run] + self._out
         self.points = sum(g.numel() for g in self.grids)
 
     def numel(self):
@@ -275,14 +295,15 @@ class HostBatch:
             raise _lib.InvalidArgument("host buffers must hold numel() "
                                        "elements in the packed layout")
         cur = stream or torch.cuda.current_stream(self.buf.device)
-        s_in, s_run, s_out = self._streams
+        s_run = self._run
         start = torch.cuda.Event()
         start.record(cur)
         for s in self._streams:
             s.wait_event(start)
         landed, done = [], []
-        with torch.cuda.stream(s_in):
-            for a, b in self.spans:
+        for i, (a, b) in enumerate(self.spans):
+            s_in = self._in[i % len(self._in)]
+            with torch.cuda.stream(s_in):
                 self.buf[a:b].copy_(host_in[a:b], non_blocking=True)
                 ev = torch.cuda.Event()
                 ev.record(s_in)
@@ -294,13 +315,15 @@ class HostBatch:
             ev2 = torch.cuda.Event()
             ev2.record(s_run)
             done.append(ev2)
-        with torch.cuda.stream(s_out):
-            for (a, b), ev in zip(self.spans, done):
+        for i, ((a, b), ev) in enumerate(zip(self.spans, done)):
+            s_out = self._out[i % len(self._out)]
+            with torch.cuda.stream(s_out):
                 s_out.wait_event(ev)
                 host_out[a:b].copy_(self.buf[a:b], non_blocking=True)
-        end = torch.cuda.Event()
-        end.record(s_out)
-        cur.wait_event(end)
+        for s_out in self._out:
+            end = torch.cuda.Event()
+            end.record(s_out)
+            cur.wait_event(end)
 
     def close(self):
         for bt in self.batches:

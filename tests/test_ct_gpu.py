@@ -336,3 +336,84 @@ def test_autotune_keeps_results_exact():
                 want = O.hierarchize(xi.copy(), lv, lmin, lmax, "biorthogonal")
                 assert np.array_equal(got, want), lv
         b.close()
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("coefficients", ["integer", "fraction"])
+def test_combine_restrict_subspaces_in_many_grids(dtype, coefficients):
+    """1100 small 4D grids (levels 1..3 per dimension, repeated level
+    vectors allowed): the sums over the grids run in grid order, so they
+    equal the oracle's bit for bit. Integer coefficients on FP32 grids take
+    the fused multiply-add (exact products), fractions the separately
+    rounded form. The coarsest subspaces lie in more than 1024 grids and are
+    restricted one warp per point, the rest one thread per point; restrict
+    writes every grid's copy of every subspace."""
+    import torch
+    rng = np.random.default_rng(11)
+    levels = [tuple(int(x) for x in rng.integers(1, 4, 4))
+              for _ in range(1100)]
+    if coefficients == "integer":
+        coeffs = [float(c) for c in rng.integers(-3, 4, len(levels))]
+    else:
+        coeffs = [float(c) for c in rng.uniform(-1, 1, len(levels))]
+    lmax = (3, 3, 3, 3)
+    xs = [rng.uniform(-1, 1, [1 << l for l in lv]).astype(dtype)
+          for lv in levels]
+    gs = upload(xs)
+    ct = pct.CombinationTechnique(gs, levels, coeffs, lmax)
+    O = oracle()
+    subs, offs = ct.subspaces()
+    counts = O.subspace_counts(levels)
+    assert max(counts[s] for s in subs) > 1024
+    assert any(counts[s] <= 1024 for s in subs)
+    sparse = ct.combine()
+    torch.cuda.synchronize()
+    want = O.combine([x.astype(np.float64) for x in xs], levels, coeffs,
+                     lmax, subs)
+    got = sparse.cpu().numpy()
+    for w, off in zip(want, offs):
+        assert np.array_equal(got[off:off + w.size], w.reshape(-1))
+    ct.restrict(sparse)
+    torch.cuda.synchronize()
+    sp = sparse.cpu().numpy().astype(dtype)
+    for g, lv, x in zip(gs, levels, xs):
+        arr = g.cpu().numpy().reshape(x.shape)
+        for s, off in zip(subs, offs):
+            if any(si > li for si, li in zip(s, lv)):
+                continue
+            n = O.subspace_size(s)
+            assert np.array_equal(arr[O.subspace_slices(s, lv)].reshape(-1),
+                                  sp[off:off + n])
+    ct.close()
+
+
+@pytest.mark.parametrize("groups", [1, 2, 3, 7, 20])
+def test_batch_groups_give_identical_results(groups):
+    """Grids dealt into groups run on parallel branches (forked streams,
+    joined into the caller's stream, captured into one graph); every group
+    count gives the oracle's values bit for bit, through a graph on a
+    non-default stream and through direct launches on the legacy stream,
+    including long pencils with shadow-buffer stages in every group."""
+    import torch
+    levels = [(14, 2), (2, 14), (13, 3), (3, 13), (8, 8), (9, 7), (7, 9),
+              (12, 4), (4, 12), (6, 6), (5, 5), (1, 1)]
+    lmin, lmax = (1, 1), (14, 14)
+    rng = np.random.default_rng(groups)
+    xs = [rng.uniform(-1, 1, [1 << l for l in lv]) for lv in levels]
+    gs = upload(xs)
+    b = pct.Batch(gs, levels, lmin, lmax, "biorthogonal", groups=groups)
+    O = oracle()
+    s = torch.cuda.Stream()
+    for _ in range(2):  # capture, then replay
+        for g, x in zip(gs, xs):
+            g.copy_(torch.from_numpy(x).reshape(-1))
+        b.hierarchize(s)
+        s.synchronize()
+        for g, x, lv in zip(gs, xs, levels):
+            want = O.hierarchize(x.copy(), lv, lmin, lmax, "biorthogonal")
+            assert np.array_equal(g.cpu().numpy().reshape(want.shape), want)
+    b.dehierarchize()  # legacy default stream: forked direct launches
+    torch.cuda.synchronize()
+    for g, x in zip(gs, xs):
+        assert np.max(np.abs(g.cpu().numpy().reshape(x.shape) - x)) <= 1e-13
+    b.close()

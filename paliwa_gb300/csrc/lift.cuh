@@ -190,6 +190,27 @@ __device__ __forceinline__ int stage_pitch(int G) {
   return (G * (R + 1)) | 1;
 }
 
+// Column pitch of a staged tile of 2^log2cols columns of G chunks. Narrow
+// rows of RL = min(inner extent, columns) <= 2^kNarrowRowLog2 elements are
+// loaded with consecutive lanes along a row (TileCopy::rows_load), so a warp
+// covers RL columns of 32 / RL consecutive rows. With G >= 32 a warp's chunk
+// reads lie in one column and the pitch does not matter to them; then
+// pitch = 32 / RL (mod 32) puts the warp's copies at banks q * 32 / RL + r,
+// all distinct (an odd pitch would give conflicts). Otherwise the pitch is
+// odd (stage_pitch). The tile still fits lift_smem_bytes: the pitch grows by
+// at most 31 and cols <= rounds * NT / 32.
+constexpr int kNarrowRowLog2 = 3;  // rows of up to 8 elements: rows_load
+
+template <int R, typename S>
+__device__ __forceinline__ int tile_pitch(int G, int log2_inner,
+                                          int log2cols, bool contiguous) {
+  int const base = G * (R + 1);
+  int const log2RL = log2_inner < log2cols ? log2_inner : log2cols;
+  if (G < 32 || contiguous || log2RL > kNarrowRowLog2) return base | 1;
+  int const want = 32 >> log2RL;
+  return base + ((want - base) & 31);
+}
+
 // Exchanges between the chunks of one column during the level steps of a
 // round. When G <= 32 the chunks of a column are lanes of one warp and
 // exchange by shuffle: chunk c is lane (lane & ~mask) | (c << log2ls) with
@@ -719,6 +740,64 @@ template <typename S, int R, int NT> struct TileCopy {
            seg * seg_len + (k - halo) < n;
   }
 
+  // True when the tile is copied along k as 16-byte vectors (each column a
+  // contiguous pencil: the last axis); otherwise row by row.
+  static __device__ __forceinline__ bool contiguous(LiftJob const &j) {
+    bool const aligned = ((j.base | j.dst_base) & 15ull) == 0;
+    return aligned && VEC > 1 && j.log2_inner == 0 && j.log2_kstride == 0 &&
+           R >= VEC;
+  }
+
+  // Row-wise load of narrow rows (RL = 2^log2RL <= 2^kNarrowRowLog2
+  // elements; row rho = (a_off, k)): one element per lane and step with
+  // consecutive lanes along a row, so a warp's 32 asynchronous copies read
+  // 32 / RL rows and, with tile_pitch, write 32 distinct banks. Copying a
+  // whole vector per lane (rows) would touch 32 rows per instruction, as the
+  // elements of a vector land `pitch` apart and each is one copy. When the
+  // tile lies in one outer slab (inner >= cols, so a_off = 0) of a periodic
+  // job, consecutive steps are a constant number of rows apart, a multiple
+  // of R: addresses advance by constants.
+  __device__ __forceinline__ void rows_load(S *stage, int t,
+                                            int log2RL) const {
+    constexpr int PER = kTileRounds * R;  // elements per thread
+    S const *const g = reinterpret_cast<S const *>(gbase);
+    int const log2B = job.log2_inner;
+    long long const base = ((gc0 >> log2B) << job.log2_astride) +
+                           (gc0 & ((1LL << log2B) - 1));
+    long long const room = job.columns - gc0;  // columns left in the job
+    int const rmask = (1 << log2RL) - 1;
+    int const q = t & rmask;  // the same in every step: NT is a multiple
+    if (periodic && log2B >= 31 - __clz(cols)) {
+      if (q >= room) return;
+      int const drho = NT >> log2RL;  // rows per step, a multiple of R
+      int const k0 = t >> log2RL;
+      long long off = base + (static_cast<long long>(k0) << job.log2_kstride) + q;
+      long long const doff = static_cast<long long>(drho) << job.log2_kstride;
+      int sb = sidx(q, k0);
+      int const dsb = (drho >> LOG2R) * (R + 1);
+#pragma unroll 8
+      for (int i = 0; i < PER; ++i) {
+        cp_async<sizeof(S)>(stage + sb, g + off);
+        off += doff;
+        sb += dsb;
+      }
+      return;
+    }
+    int const kmask = (1 << log2W) - 1;
+#pragma unroll 4
+    for (int i = 0; i < PER; ++i) {
+      int const rho = (t + i * NT) >> log2RL;
+      int const k = rho & kmask;
+      int const a_off = rho >> log2W;
+      int const w = (a_off << log2RL) + q;
+      if (w >= room) continue;
+      long long const off =
+          base + (static_cast<long long>(a_off) << job.log2_astride) +
+          (pos(k) << job.log2_kstride) + q;
+      cp_async<sizeof(S)>(stage + sidx(w, k), g + off);
+    }
+  }
+
   // Rows of RL = min(inner, cols) contiguous elements; row rho = (a_off, k);
   // VW elements per memory access (VW * sizeof(S) <= 16 bytes). A tile holds
   // exactly NT * PER vectors, and every thread issues all of its loads before
@@ -812,6 +891,9 @@ template <typename S, int R, int NT> struct TileCopy {
       return;
     }
     int const log2RL = log2B < log2cols ? log2B : log2cols;
+    if constexpr (!Store) {
+      if (log2RL <= kNarrowRowLog2) return rows_load(stage, t, log2RL);
+    }
     // Vector width: as wide as the rows and the alignment allow.
     if constexpr (VEC >= 4) {
       if (aligned && log2RL >= 2)
@@ -901,7 +983,10 @@ __global__ void __launch_bounds__(NT)
     int const log2CR = LOG2NT - log2G;        // columns per round
     constexpr int rounds = kTileRounds;
     int const cols = rounds << log2CR;        // columns per tile
-    int const pitch = stage_pitch<R>(G);
+    int const pitch = tile_pitch<R, typename A::Store>(
+        G, job->log2_inner, LOG2NT - log2G + 1,
+        TileCopy<typename A::Store, R, NT>::contiguous(*job));
+    static_assert(kTileRounds == 2, "tile_pitch takes log2(cols) = log2CR + 1");
     int const periodic = job->periodic;
     long long const n = 1LL << job->log2_n;
 

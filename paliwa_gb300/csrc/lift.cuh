@@ -754,9 +754,9 @@ template <typename S, int R, int NT> struct TileCopy {
   // 32 / RL rows and, with tile_pitch, write 32 distinct banks. Copying a
   // whole vector per lane (rows) would touch 32 rows per instruction, as the
   // elements of a vector land `pitch` apart and each is one copy. When the
-  // tile lies in one outer slab (inner >= cols, so a_off = 0) of a periodic
-  // job, consecutive steps are a constant number of rows apart, a multiple
-  // of R: addresses advance by constants.
+  // tile lies in one outer slab (inner >= cols, so a_off = 0), consecutive
+  // steps are a constant number of rows apart, a multiple of R: addresses
+  // advance by constants (for windows, modulo the pencil length).
   __device__ __forceinline__ void rows_load(S *stage, int t,
                                             int log2RL) const {
     constexpr int PER = kTileRounds * R;  // elements per thread
@@ -767,18 +767,19 @@ template <typename S, int R, int NT> struct TileCopy {
     long long const room = job.columns - gc0;  // columns left in the job
     int const rmask = (1 << log2RL) - 1;
     int const q = t & rmask;  // the same in every step: NT is a multiple
-    if (periodic && log2B >= 31 - __clz(cols)) {
+    if (log2B >= 31 - __clz(cols)) {
       if (q >= room) return;
       int const drho = NT >> log2RL;  // rows per step, a multiple of R
       int const k0 = t >> log2RL;
-      long long off = base + (static_cast<long long>(k0) << job.log2_kstride) + q;
-      long long const doff = static_cast<long long>(drho) << job.log2_kstride;
+      long long pk = pos(k0);  // pencil position of row k0 + i * drho
       int sb = sidx(q, k0);
       int const dsb = (drho >> LOG2R) * (R + 1);
+      S const *const gq = g + base + q;
 #pragma unroll 8
       for (int i = 0; i < PER; ++i) {
-        cp_async<sizeof(S)>(stage + sb, g + off);
-        off += doff;
+        cp_async<sizeof(S)>(stage + sb, gq + (pk << job.log2_kstride));
+        pk += drho;
+        if (pk >= n) pk -= n;  // a window wrapping around the period
         sb += dsb;
       }
       return;
@@ -1107,6 +1108,34 @@ struct WideUnit {
   bool keep;      // the thread's column group is in range (else recomputed)
 };
 
+// Strided wide units whose inner extent is one or two row vectors (kCols or
+// 2 kCols columns) while a warp holds more column groups than that: each
+// lane's rows then lie in slabs of other outer indices than its neighbours',
+// so copying row by row touches 16 to 32 lines per instruction. The warp's
+// columns cover whole slabs, which lie contiguously in memory: such warps
+// copy their block (32 * R row vectors) as consecutive 16-byte pieces
+// instead, into their shared-memory region with an XOR swizzle of the piece
+// index (piece b at b ^ ((b >> 3) & 7): the 8 pieces of a 128-byte line
+// rotate with the line), and each thread reads its rows from there. With
+// wider inner extents the row-by-row copy touches 8 lines or fewer and its
+// fewer instructions win (measured: block copies for inner extents up to
+// 32 kCols made the 4D CT step 2 % slower). Only the 16-point units use it:
+// for R = 4 and 8 its address work cost more than the copies it saved.
+struct WideBlock {
+  static __device__ __forceinline__ bool use(LiftJob const &job,
+                                             WideUnit const &w, int log2gw,
+                                             int log2cw) {
+    return job.log2_inner <= log2cw + 1 && log2cw + 1 < log2gw + log2cw &&
+           job.log2_kstride == job.log2_inner &&
+           job.log2_astride == job.log2_n + job.log2_inner &&
+           w.wfirst + (1LL << log2gw) <= w.groups &&
+           ((job.base | job.dst_base) & 15ull) == 0;
+  }
+  static __device__ __forceinline__ int swz(int b) {
+    return b ^ ((b >> 3) & 7);
+  }
+};
+
 template <int LOG2R, int LOG2NT, int LOG2CW, bool Contig>
 __device__ __forceinline__ WideUnit wide_unit(LiftJob const &job,
                                               long long unit, int t) {
@@ -1339,13 +1368,39 @@ __global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
           if (over > 0) o -= over << log2blk;
           cp_async<16>(wslots + CP::slot(owner, pc), wsrc + o);
         }
-      } else {
+      } else if constexpr (R < 16) {
+        // Pencils of up to 8 points: row by row (the block copy's extra
+        // address work measured slower for these issue-bound units).
         E const *const src = reinterpret_cast<E const *>(job.base) + w.off;
         W *const dst = reinterpret_cast<W *>(st) + t;
         long long const kstride = 1LL << job.log2_kstride;
 #pragma unroll
         for (int j = 0; j < R; ++j)
           cp_async<sizeof(W)>(dst + j * NT, src + j * kstride);
+      } else {
+        // The warp's region of the stage: 32 * R row vectors.
+        unsigned char *const wreg = st + (t >> 5) * (32 * SLOT_BYTES);
+        int const log2gw = 5 - (job.log2_n - LOG2R);
+        if (WideBlock::use(job, w, log2gw, LOG2CW)) {
+          constexpr int PL = SLOT_BYTES / 16;  // pieces per lane
+          constexpr int LOG2E16 = Log2<16 / sizeof(E)>::value;
+          long long const slab0 = (w.wfirst << LOG2CW) >> job.log2_inner;
+          E const *const bsrc = reinterpret_cast<E const *>(job.base) +
+                                (slab0 << job.log2_astride);
+#pragma unroll
+          for (int i = 0; i < PL; ++i) {
+            int const b = i * 32 + lane;
+            cp_async<16>(wreg + (WideBlock::swz(b) << 4),
+                         bsrc + (static_cast<long long>(b) << LOG2E16));
+          }
+        } else {
+          E const *const src = reinterpret_cast<E const *>(job.base) + w.off;
+          W *const dst = reinterpret_cast<W *>(wreg) + lane;
+          long long const kstride = 1LL << job.log2_kstride;
+#pragma unroll
+          for (int j = 0; j < R; ++j)
+            cp_async<sizeof(W)>(dst + j * 32, src + j * kstride);
+        }
       }
     }
     cp_async_commit();
@@ -1385,10 +1440,34 @@ __global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
         memcpy(&x, row, sizeof(W));
         v[j] = A::load(x);
       }
-    } else {
+    } else if constexpr (R < 16) {
 #pragma unroll
       for (int j = 0; j < R; ++j)
         v[j] = A::load(reinterpret_cast<W const *>(st)[j * NT + t]);
+    } else {
+      unsigned char const *const wreg = st + (t >> 5) * (32 * SLOT_BYTES);
+      int const log2gw = 5 - (job.log2_n - LOG2R);
+      if (WideBlock::use(job, w, log2gw, LOG2CW)) {
+        // Element offset of the thread's chunk of its column group in the
+        // block: slab gl * kCols / inner, column gl * kCols mod inner.
+        int const gl = lane & ((1 << log2gw) - 1);
+        int const log2B = job.log2_inner;
+        int const e0 = (((gl << LOG2CW) >> log2B) << (job.log2_n + log2B)) +
+                       ((w.c << LOG2R) << log2B) +
+                       ((gl << LOG2CW) & ((1 << log2B) - 1));
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+          int const byte = (e0 + (j << log2B)) * static_cast<int>(sizeof(E));
+          W x;
+          memcpy(&x, wreg + (WideBlock::swz(byte >> 4) << 4) + (byte & 15),
+                 sizeof(W));
+          v[j] = A::load(x);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+          v[j] = A::load(reinterpret_cast<W const *>(wreg)[j * 32 + lane]);
+      }
     }
     int const log2G = job.log2_n - LOG2R;
     RoundCtx<A, NT> ctx(t, w.c, 1 << log2G, log2G, lane, 1, nullptr, nullptr,

@@ -25,13 +25,18 @@ compared with the FP64 one (normwise max / rms error, overall and per q).
 buffers and the host<->device copies inside the timed region. ``roofline``
 is the dominant lifting launch: algorithmic bytes (one read and one write of
 each grid point it stores) over its CUDA-event duration, from an event-
-bracketed pass over the same plan. ``--impl reference`` times the
+bracketed pass over the same plan; ``roofline.step_frac`` is the whole
+step's algorithmic traffic over the graph-timed step (with the batch's
+groups running concurrently). ``--impl reference`` times the
 reference's CPU algorithm (the oracle port in oracle/; the reference itself
 needs DDC and Kokkos, which are absent) on all host cores.
 
 For N > 1 (torchrun), each rank transforms an independent replica of the
 workload ("replicas only"); value sums the ranks' points over the slowest
 rank's time.
+
+``--probe-axis LEVELS:DIM:MODE`` instead times one axis of one random grid
+(used for single-kernel captures).
 """
 from __future__ import annotations
 
@@ -368,6 +373,35 @@ def time_steps(fwd, inv, steps, warmup, stream, world):
     return s.elapsed_time(e)
 
 
+def bind_to_gpu_numa_node(index):
+    """Restricts this process to the host cores of the NUMA node of CUDA
+    device `index` (from its PCI address in sysfs). Returns the node, or
+    None where the topology is not exposed (the affinity is then left as
+    it is)."""
+    import torch
+    try:
+        p = torch.cuda.get_device_properties(index)
+        bus = "%04x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id,
+                                    p.pci_device_id)
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            node = int(f.read())
+        if node < 0:
+            return None
+        with open(f"/sys/devices/system/node/node{node}/cpulist") as f:
+            spec = f.read().strip()
+        cpus = set()
+        for part in spec.split(","):
+            a, _, b = part.partition("-")
+            cpus.update(range(int(a), int(b or a) + 1))
+        cpus &= os.sched_getaffinity(0)
+        if not cpus:
+            return None
+        os.sched_setaffinity(0, cpus)
+        return node
+    except (AttributeError, OSError, ValueError):
+        return None
+
+
 def run_gpu(args, w, world, rank, local):
     import numpy as np
     import torch
@@ -563,9 +597,17 @@ def run_gpu(args, w, world, rank, local):
     hb = pct.HostBatch(w.levels, w.lmin, w.lmax, w.wavelet, torch.float32,
                        compensated=True, groups=E2E_GROUPS, device=dev,
                        batch_groups=1, copy_streams=E2E_COPY_STREAMS)
+    # Pinned buffers in the host memory next to the GPU's host link: they
+    # are allocated (and so placed) while this process runs on the cores of
+    # the GPU's NUMA node; the full affinity is restored afterwards.
+    saved = os.sched_getaffinity(0) if hasattr(os, "sched_getaffinity") \
+        else None
+    numa = bind_to_gpu_numa_node(local)
     host_in = torch.empty(hb.numel(), dtype=torch.float32).pin_memory()
-    host_in.copy_(b32)
     host_out = torch.empty_like(host_in).pin_memory()
+    if saved is not None:
+        os.sched_setaffinity(0, saved)
+    host_in.copy_(b32)
     del b32, v32
 
     def e2e_step():
@@ -618,20 +660,53 @@ def run_gpu(args, w, world, rank, local):
                 "bytes_per_launch": top_b / top_n,
                 "launch_ms": top_ms / top_n,
                 "all_launches_frac":
-                    tot32_b / (tot32_ms / 1e3) / 1e9 / peak},
+                    tot32_b / (tot32_ms / 1e3) / 1e9 / peak,
+                # The step itself: every launch's algorithmic bytes of one
+                # forward + inverse over the graph-timed step (the groups'
+                # launches overlap there; all_launches_frac times them one
+                # by one).
+                "step_frac":
+                    tot32_b / (ms32 / args.steps / 1e3) / 1e9 / peak},
             "combine": combine,
             "autotune": tuning,
             "clocks": clocks.summary(),
             "e2e": {"value": e2e_value, "unit": "points/s",
                     "h2d_bytes_per_step": e2e_bytes,
                     "d2h_bytes_per_step": e2e_bytes,
-                    "groups": E2E_GROUPS},
+                    "groups": E2E_GROUPS, "host_numa_node": numa},
             "gpu_launches": args.steps * nlaunch,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
     bt32.close()
     bt64.close()
+
+
+def run_axis_probe(spec):
+    """One axis of one grid, for kernel captures: ``LEVELS:DIM:MODE`` (e.g.
+    ``12,7,7:0:f32c``; MODE f64, f32 or f32c) runs hierarchize_in along DIM
+    of a random grid twice (CDF biorthogonal, lmin 0) and prints the second
+    run's event-timed milliseconds and algorithmic GB/s."""
+    import torch
+
+    import paliwa_gb300 as pg
+    lv, dim, mode = spec.split(":")
+    level = tuple(int(x) for x in lv.split(","))
+    dim = int(dim)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    g = torch.rand([1 << l for l in level], dtype=dt, device="cuda")
+    lmin = (0,) * len(level)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for r in range(2):
+        if r == 1:
+            ev[0].record()
+        pg.hierarchize_in(g, dim, level, lmin, level, "biorthogonal",
+                          compensated=(mode == "f32c"))
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1])
+    gbs = 2 * g.numel() * g.element_size() / ms / 1e6
+    print(json.dumps({"probe": spec, "ms": ms, "GB/s": gbs}), flush=True)
 
 
 def main():
@@ -650,7 +725,13 @@ def main():
     ap.add_argument("--launch-table", action="store_true",
                     help="print the plan's launches (kernel, algorithmic "
                          "bytes, event-timed ms) to stderr")
+    ap.add_argument("--probe-axis", metavar="LEVELS:DIM:MODE",
+                    help="time one axis of one grid instead (for kernel "
+                         "captures), e.g. 12,7,7:0:f32c")
     args = ap.parse_args()
+    if args.probe_axis:
+        run_axis_probe(args.probe_axis)
+        return
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
     w = Workload(args.workload)

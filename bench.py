@@ -254,6 +254,18 @@ def max_over_ranks(world, value):
     return float(t.item())
 
 
+def step_bytes(w, elem):
+    """Algorithmic bytes of one step (forward + inverse): a read and a
+    write of every grid point per axis that has levels to transform
+    (level > minimum level)."""
+    total = 0
+    for lv in w.levels:
+        n = 1 << sum(lv)
+        total += sum(2 * n * elem for d in range(len(lv))
+                     if lv[d] > w.lmin[d])
+    return 2 * total
+
+
 def config_of(w, args):
     c = {"workload": w.name, "grids": len(w.levels), "points": w.points,
          "ndim": w.ndim, "minimum_level": list(w.lmin),
@@ -661,12 +673,15 @@ def run_gpu(args, w, world, rank, local):
                 "launch_ms": top_ms / top_n,
                 "all_launches_frac":
                     tot32_b / (tot32_ms / 1e3) / 1e9 / peak,
-                # The step itself: every launch's algorithmic bytes of one
-                # forward + inverse over the graph-timed step (the groups'
-                # launches overlap there; all_launches_frac times them one
-                # by one).
-                "step_frac":
-                    tot32_b / (ms32 / args.steps / 1e3) / 1e9 / peak},
+                # The step itself: its algorithmic bytes (one read and one
+                # write of every point per transformed axis and direction;
+                # axes at the minimum level have no levels and move
+                # nothing; the long pencils' copy stages are not counted)
+                # over the graph-timed step (the groups' launches overlap
+                # there; all_launches_frac times them one by one).
+                "step_bytes": step_bytes(w, 4),
+                "step_frac": step_bytes(w, 4) /
+                    (ms32 / args.steps / 1e3) / 1e9 / peak},
             "combine": combine,
             "autotune": tuning,
             "clocks": clocks.summary(),

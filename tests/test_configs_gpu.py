@@ -125,3 +125,50 @@ def test_c4_full_size_round_trip_and_fp32c_error():
     bt64.close()
     bt32.close()
     assert math.isfinite(err)
+
+
+def test_c5_ct_pipeline_per_q_error():
+    """C5: the 6D CDF (2,2) scheme |l|_1 = 16 - q, q = 0..5 (7,798 grids,
+    292 M points): forward transform of every grid, FP64 combine into the
+    sparse grid, restrict back, inverse of every grid. The FP32-compensated
+    pipeline (FP32 grids, combine still in FP64) is held to the FP64
+    pipeline per q, normwise (max |e| / max |ref| <= 1e-6); the FP64
+    pipeline's combine is exact in its order (checked bit for bit on small
+    schemes in test_ct_gpu.py), so the FP64 results here are the
+    reference values."""
+    import torch
+    import bench
+    from paliwa_gb300 import ct as pct
+    w = bench.Workload("6d-ct-16")
+    b64, v64 = pct.packed_grids(w.levels, torch.float64)
+    for i, v in enumerate(v64):
+        v.copy_(torch.from_numpy(np.ascontiguousarray(
+            w.grid_values(i)).reshape(-1)))
+    b32, v32 = pct.packed_grids(w.levels, torch.float32)
+    b32.copy_(b64)
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    out = {}
+    for name, grids, comp in (("f64", v64, False), ("f32c", v32, True)):
+        bt = pct.Batch(grids, w.levels, w.lmin, w.lmax, w.wavelet,
+                       compensated=comp)
+        ct = pct.CombinationTechnique(grids, w.levels, w.coeffs, w.lmax)
+        bt.hierarchize(s)
+        sparse = ct.combine(stream=s)
+        ct.restrict(sparse, stream=s)
+        bt.dehierarchize(s)
+        s.synchronize()
+        out[name] = sparse.clone()
+        ct.close()
+        bt.close()
+    ref = out["f64"]
+    assert torch.isfinite(out["f32c"]).all()
+    assert torch.isfinite(ref).all()
+    # Per q, over the grids of that q, after the inverse.
+    for q in sorted(set(w.q)):
+        idx = [i for i, qq in enumerate(w.q) if qq == q]
+        a = torch.cat([v32[i].double() for i in idx])
+        b = torch.cat([v64[i] for i in idx])
+        rel = float((a - b).abs().max()) / float(b.abs().max())
+        assert rel <= 1e-6, (q, rel)
+        assert math.isfinite(rel)

@@ -51,7 +51,6 @@ struct Direction {
   std::vector<Launch> launches;
   LiftJob *jobs_dev = nullptr;
   cudaGraphExec_t graph = nullptr;
-  cudaStream_t graph_stream = nullptr;
   Tuning tuning;  // kernel forced per class (autotuner)
   // Classes of the plan's periodic stages: applicable kernels (bits), the
   // default choice of the first stage seen, and the points they store.

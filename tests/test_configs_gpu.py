@@ -131,11 +131,15 @@ def test_c5_ct_pipeline_per_q_error():
     """C5: the 6D CDF (2,2) scheme |l|_1 = 16 - q, q = 0..5 (7,798 grids,
     292 M points): forward transform of every grid, FP64 combine into the
     sparse grid, restrict back, inverse of every grid. The FP32-compensated
-    pipeline (FP32 grids, combine still in FP64) is held to the FP64
-    pipeline per q, normwise (max |e| / max |ref| <= 1e-6); the FP64
-    pipeline's combine is exact in its order (checked bit for bit on small
-    schemes in test_ct_gpu.py), so the FP64 results here are the
-    reference values."""
+    pipeline (FP32 grids, combine still in FP64) is compared per q with the
+    FP64 pipeline, normwise (max |e| / max |ref| over the grids of that q).
+
+    The combination adds grids with coefficients up to C(5, 2) = 10, which
+    amplifies the rounding of the inputs to FP32 storage: the FP64 pipeline
+    run on the FP32-rounded inputs is already 1.5e-6 to 2.4e-6 away (the
+    storage floor), above 1e-6. The FP32c pipeline (measured 3.0e-6 to
+    3.8e-6, 1.6 to 2.1 times the floor) is held to three times that floor
+    per q; its forward transform alone to 1e-6."""
     import torch
     import bench
     from paliwa_gb300 import ct as pct
@@ -144,31 +148,45 @@ def test_c5_ct_pipeline_per_q_error():
     for i, v in enumerate(v64):
         v.copy_(torch.from_numpy(np.ascontiguousarray(
             w.grid_values(i)).reshape(-1)))
+    pristine = b64.clone()
     b32, v32 = pct.packed_grids(w.levels, torch.float32)
-    b32.copy_(b64)
     torch.cuda.synchronize()
     s = torch.cuda.Stream()
-    out = {}
-    for name, grids, comp in (("f64", v64, False), ("f32c", v32, True)):
-        bt = pct.Batch(grids, w.levels, w.lmin, w.lmax, w.wavelet,
-                       compensated=comp)
-        ct = pct.CombinationTechnique(grids, w.levels, w.coeffs, w.lmax)
+    bt64 = pct.Batch(v64, w.levels, w.lmin, w.lmax, w.wavelet)
+    ct64 = pct.CombinationTechnique(v64, w.levels, w.coeffs, w.lmax)
+    bt32 = pct.Batch(v32, w.levels, w.lmin, w.lmax, w.wavelet,
+                     compensated=True)
+    ct32 = pct.CombinationTechnique(v32, w.levels, w.coeffs, w.lmax)
+
+    def pipeline(bt, ct, buf, inputs, forward_only=False):
+        buf.copy_(inputs)
+        torch.cuda.synchronize()
         bt.hierarchize(s)
-        sparse = ct.combine(stream=s)
-        ct.restrict(sparse, stream=s)
-        bt.dehierarchize(s)
+        if not forward_only:
+            sparse = ct.combine(stream=s)
+            ct.restrict(sparse, stream=s)
+            bt.dehierarchize(s)
         s.synchronize()
-        out[name] = sparse.clone()
-        ct.close()
-        bt.close()
-    ref = out["f64"]
-    assert torch.isfinite(out["f32c"]).all()
-    assert torch.isfinite(ref).all()
-    # Per q, over the grids of that q, after the inverse.
-    for q in sorted(set(w.q)):
+        return buf.double().clone()
+
+    ref = pipeline(bt64, ct64, b64, pristine)
+    floor = pipeline(bt64, ct64, b64, pristine.float().double())
+    got = pipeline(bt32, ct32, b32, pristine)
+    starts = [(v.data_ptr() - b64.data_ptr()) // 8 for v in v64]
+
+    def per_q(a, q):
         idx = [i for i, qq in enumerate(w.q) if qq == q]
-        a = torch.cat([v32[i].double() for i in idx])
-        b = torch.cat([v64[i] for i in idx])
-        rel = float((a - b).abs().max()) / float(b.abs().max())
-        assert rel <= 1e-6, (q, rel)
-        assert math.isfinite(rel)
+        x = torch.cat([a[starts[i]:starts[i] + v64[i].numel()] for i in idx])
+        y = torch.cat([ref[starts[i]:starts[i] + v64[i].numel()]
+                       for i in idx])
+        return float((x - y).abs().max()) / float(y.abs().max())
+
+    for q in sorted(set(w.q)):
+        e, f = per_q(got, q), per_q(floor, q)
+        assert math.isfinite(e) and e <= 3 * f, (q, e, f)
+    fwd = pipeline(bt32, ct32, b32, pristine, forward_only=True)
+    ref_fwd = pipeline(bt64, ct64, b64, pristine, forward_only=True)
+    rel = float((fwd - ref_fwd).abs().max()) / float(ref_fwd.abs().max())
+    assert rel <= 1e-6, rel
+    for h in (ct64, ct32, bt64, bt32):
+        h.close()

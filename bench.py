@@ -35,8 +35,9 @@ For N > 1 (torchrun), each rank transforms an independent replica of the
 workload ("replicas only"); value sums the ranks' points over the slowest
 rank's time.
 
-``--probe-axis LEVELS:DIM:MODE`` instead times one axis of one random grid
-(used for single-kernel captures).
+``--probe-axis LEVELS:DIM:MODE`` instead times one axis of one random grid,
+``--probe-outputs LEVELS:DIM:MODE`` the restricted-output transform of one
+(both used for single-kernel captures).
 """
 from __future__ import annotations
 
@@ -724,6 +725,53 @@ def run_axis_probe(spec):
     print(json.dumps({"probe": spec, "ms": ms, "GB/s": gbs}), flush=True)
 
 
+def run_outputs_probe(spec):
+    """The restricted-output transform on one grid, for kernel captures:
+    ``LEVELS:DIM:MODE`` (MODE f64 or f32) hierarchizes along DIM (CDF
+    biorthogonal, every level) with outputs = the first half of the axis,
+    the whole grid as the window, twice, and prints the second run's
+    event-timed milliseconds, the points written and the algorithmic GB/s
+    of its lifting passes (three reads and one write per written point)."""
+    import torch
+
+    import paliwa_gb300 as pg
+    lv, dim, mode = spec.split(":")
+    level = tuple(int(x) for x in lv.split(","))
+    dim = int(dim)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    g = torch.rand([1 << l for l in level], dtype=dt, device="cuda")
+    filters = pg.lifting_wavelet_filter_offsets_and_coefficients[
+        "biorthogonal"]
+    levels = list(range(level[dim], 0, -1))
+    ext = [1 << l for l in level]
+    ext[dim] //= 2
+    outputs = ((0,) * len(level), ext, (1,) * len(level))
+    bounds, writes = pg.transform_bounds(
+        (0, (1 << level[dim]) // 2 - 1), level[dim], level[dim], levels,
+        filters)
+    per_col = 0
+    for i, l in enumerate(levels):
+        stride = 2 << (level[dim] - l)
+        period = 1 << level[dim]
+        for w in writes[i]:
+            if w is not None:
+                span = (w[1] - w[0]) % period
+                per_col += span // stride + 1
+    cols = g.numel() >> level[dim]
+    written = per_col * cols
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for r in range(2):
+        if r == 1:
+            ev[0].record()
+        pg.transform_outputs(g, dim, level, level, levels, filters, outputs)
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1])
+    gbs = 4 * written * g.element_size() / ms / 1e6
+    print(json.dumps({"probe_outputs": spec, "ms": ms,
+                      "points_written": written, "GB/s": gbs}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -743,9 +791,15 @@ def main():
     ap.add_argument("--probe-axis", metavar="LEVELS:DIM:MODE",
                     help="time one axis of one grid instead (for kernel "
                          "captures), e.g. 12,7,7:0:f32c")
+    ap.add_argument("--probe-outputs", metavar="LEVELS:DIM:MODE",
+                    help="time the restricted-output transform of one grid "
+                         "(outputs: half the axis), e.g. 10,8,8:0:f64")
     args = ap.parse_args()
     if args.probe_axis:
         run_axis_probe(args.probe_axis)
+        return
+    if args.probe_outputs:
+        run_outputs_probe(args.probe_outputs)
         return
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()

@@ -349,6 +349,7 @@ struct paliwa_gb_ct {
   CtGrid *grids_dev = nullptr;
   int *heavy_dev = nullptr;
   long long *heavy_first_dev = nullptr;
+  int *block_sub_dev = nullptr;
   CtParams params{};
 };
 
@@ -455,6 +456,18 @@ void build_ct(paliwa_gb_ct &ct, int64_t const *levels,
   upload(&ct.grids_dev, grids, "upload grids");
   upload(&ct.heavy_dev, heavy, "upload heavy subspaces");
   upload(&ct.heavy_first_dev, heavy_first, "upload heavy offsets");
+  // First subspace of every CTA's 256 points (the subspace holding point
+  // 256 b), so that no CTA searches the whole subspace list.
+  std::vector<int> block_sub((off + kCtBlock - 1) / kCtBlock);
+  {
+    size_t si = 0;
+    for (size_t b = 0; b < block_sub.size(); ++b) {
+      long long const first = static_cast<long long>(b) * kCtBlock;
+      while (si + 1 < subs.size() && subs[si + 1].offset <= first) ++si;
+      block_sub[b] = static_cast<int>(si);
+    }
+  }
+  upload(&ct.block_sub_dev, block_sub, "upload block subspaces");
   std::memset(&ct.params, 0, sizeof(ct.params));
   ct.params.subspaces = ct.subspaces_dev;
   ct.params.nsubspaces = static_cast<int>(subs.size());
@@ -466,6 +479,7 @@ void build_ct(paliwa_gb_ct &ct, int64_t const *levels,
     ct.params.max_level[d] = static_cast<signed char>(lmax[d]);
   ct.params.heavy = ct.heavy_dev;
   ct.params.heavy_first = ct.heavy_first_dev;
+  ct.params.block_sub = ct.block_sub_dev;
   ct.params.nheavy = static_cast<int>(heavy.size());
   ct.params.nheavy_points = nheavy_points;
   // Products c * v are exact in FP64 when c has at most 53 - 24 = 29
@@ -505,11 +519,16 @@ void ct_launch(paliwa_gb_ct const &ct, double *sparse, double *full,
   CtParams p = ct.params;
   p.sparse = sparse;
   p.full = full;
-  unsigned const blocks = static_cast<unsigned>((ct.npoints + 255) / 256);
+  unsigned const blocks =
+      static_cast<unsigned>((ct.npoints + kCtBlock - 1) / kCtBlock);
   switch (ct.dtype) {
-  case PALIWA_GB_F64: ct_kernel<double, OP><<<blocks, 256, 0, s>>>(p); break;
+  case PALIWA_GB_F64:
+    ct_kernel<double, OP><<<blocks, kCtBlock, 0, s>>>(p);
+    break;
   case PALIWA_GB_F32:
-  case PALIWA_GB_F32C: ct_kernel<float, OP><<<blocks, 256, 0, s>>>(p); break;
+  case PALIWA_GB_F32C:
+    ct_kernel<float, OP><<<blocks, kCtBlock, 0, s>>>(p);
+    break;
   default: throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
   }
   cuda_check(cudaGetLastError(), "ct_kernel launch");
@@ -801,6 +820,7 @@ int paliwa_gb_ct_create(int ndim, int ngrids, const int64_t *levels,
       cudaFree(ct->grids_dev);
       cudaFree(ct->heavy_dev);
       cudaFree(ct->heavy_first_dev);
+      cudaFree(ct->block_sub_dev);
       throw;
     }
     *out = ct.release();
@@ -875,6 +895,7 @@ void paliwa_gb_ct_destroy(paliwa_gb_ct *ct) {
   cudaFree(ct->grids_dev);
   cudaFree(ct->heavy_dev);
   cudaFree(ct->heavy_first_dev);
+  cudaFree(ct->block_sub_dev);
   delete ct;
 }
 

@@ -54,7 +54,13 @@ struct CtParams {
   long long const *heavy_first;
   int nheavy;
   long long nheavy_points;
+  // block_sub[b]: the subspace holding point kCtBlock * b (the first point
+  // of CTA b), planned on the host.
+  int const *block_sub;
 };
+
+// Points (threads) per CTA of ct_kernel.
+constexpr int kCtBlock = 256;
 
 // Grid count above which restrict writes a subspace's points one warp per
 // point (lanes over grids) instead of one thread per point: a thread would
@@ -102,19 +108,6 @@ __device__ __forceinline__ long long ct_offset(long long p,
   return off;
 }
 
-__device__ __forceinline__ int ct_find_subspace(CtParams const &p,
-                                                long long point) {
-  int lo = 0, hi = p.nsubspaces - 1;
-  while (lo < hi) {
-    int const mid = (lo + hi + 1) >> 1;
-    if (p.subspaces[mid].offset <= point)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
 // Combined value of one sparse point: sum over the containing grids, in
 // grid order, of coefficient * value. One grid per iteration: loading
 // several grids ahead (8 per batch: 64 registers) measured slower on the 4D
@@ -141,15 +134,14 @@ __device__ __forceinline__ double ct_combine_point(CtParams const &p,
 enum CtOp { kCombine = 0, kRestrict = 1, kScatter = 2 };
 
 template <typename S, int OP>
-__global__ void __launch_bounds__(256) ct_kernel(CtParams const p) {
-  long long const first = static_cast<long long>(blockIdx.x) * blockDim.x;
-  if (first >= p.npoints) return;
-  // One search per CTA; threads walk forward from the CTA's first subspace.
-  __shared__ int sub0;
-  if (threadIdx.x == 0) sub0 = ct_find_subspace(p, first);
-  __syncthreads();
+__global__ void __launch_bounds__(kCtBlock) ct_kernel(CtParams const p) {
+  long long const first = static_cast<long long>(blockIdx.x) * kCtBlock;
   long long const point = first + threadIdx.x;
   if (point >= p.npoints) return;
+  // The CTA's first subspace comes from the host's table (a search of the
+  // whole list per CTA, behind a barrier, measured as the combine's second
+  // stall reason).
+  int const sub0 = p.block_sub[blockIdx.x];
   // Most CTAs lie inside one subspace: one load settles that. Otherwise
   // the CTA's 256 points span at most 256 subspaces (each has at least one
   // point): a binary search over those, instead of a walk that is as long
@@ -157,7 +149,7 @@ __global__ void __launch_bounds__(256) ct_kernel(CtParams const p) {
   int sub = sub0;
   if (sub0 + 1 < p.nsubspaces && p.subspaces[sub0 + 1].offset <= point) {
     int lo = sub0 + 1;
-    int hi = min(sub0 + static_cast<int>(blockDim.x) - 1, p.nsubspaces - 1);
+    int hi = min(sub0 + kCtBlock - 1, p.nsubspaces - 1);
     while (lo < hi) {
       int const mid = (lo + hi + 1) >> 1;
       if (p.subspaces[mid].offset <= point)

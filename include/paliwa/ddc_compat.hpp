@@ -57,6 +57,9 @@ template <class... Tags> struct DiscreteElement {
   constexpr DiscreteElement() = default;
   constexpr explicit DiscreteElement(std::array<long, sizeof...(Tags)> a)
       : uid_(a) {}
+  template <class I, class = std::enable_if_t<std::is_integral_v<I> &&
+                                              sizeof...(Tags) == 1>>
+  constexpr explicit DiscreteElement(I i) : uid_{static_cast<long>(i)} {}
   template <class T> constexpr long uid() const {
     return uid_[detail::index_of<T, Tags...>()];
   }

@@ -268,7 +268,7 @@ void for_each_transform_index(std::vector<PeriodicBounds> const &bounds,
     long const stride = h == 0 ? period : 2L << (maximum_level - h);
     long const last = b.max + (b.min > b.max ? period : 0);
     for (long x = b.min; x <= last; x += stride)
-      visit(ddc::DiscreteElement<Dim>(std::array<long, 1>{x % period}));
+      visit(ddc::DiscreteElement<Dim>(x % period));
   }
 }
 

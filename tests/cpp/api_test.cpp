@@ -91,6 +91,20 @@ int main() {
       paliwa::pole_pass_segments({0, 0}, 0, std::numeric_limits<int>::digits,
                                  std::numeric_limits<int>::digits, 1);
     }));
+    // for_each_transform_index visits every uid of the planned bounds once
+    // (paliwa_domains.hpp:454-469): outputs 4..7 of a 16-point hat
+    // hierarchization need uids 0 and 4..8.
+    {
+      paliwa::LiftingPasses const hat{{1, {-0.5, 1.0, -0.5}}};
+      auto const b = paliwa::transform_bounds(
+          {4, 7}, 4, 4, std::vector<long>{4, 3, 2, 1}, hat, ignore);
+      std::vector<int> seen(16, 0);
+      paliwa::for_each_transform_index<X>(b, 4, [&](ddc::DiscreteElement<X> e) {
+        ++seen[static_cast<size_t>(e.uid<X>())];
+      });
+      for (int u = 0; u < 16; ++u)
+        EXPECT(seen[static_cast<size_t>(u)] == ((u == 0 || (u >= 4 && u <= 8)) ? 1 : 0));
+    }
     // A window holding uids 0..7 of a 16-point axis cannot give outputs
     // 4..7 of the full hierarchization: their inputs wrap to 8..15.
     using V1 = ddc::DiscreteVector<X>;

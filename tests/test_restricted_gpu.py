@@ -20,9 +20,10 @@ WAVELET_PASSES = [
 ]
 
 
-def random_case(rng, dtype):
-    nd = rng.randint(1, 3)
-    level = [rng.randint(1, 7 if nd == 1 else 5) for _ in range(nd)]
+def random_case(rng, dtype, max_dims=3):
+    nd = rng.randint(1, max_dims)
+    level = [rng.randint(1, 7 if nd == 1 else (5 if nd <= 3 else 3))
+             for _ in range(nd)]
     maximum = [l + rng.randint(0, 2) for l in level]
     dim = rng.randrange(nd)
     lmin = rng.randrange(level[dim])
@@ -116,6 +117,14 @@ def test_random_windows_match_oracle(dtype):
                                            c["front"], c["buf"].shape)
 
 
+def test_random_windows_up_to_5d():
+    rng = random.Random(5)
+    for trial in range(60):
+        c = random_case(rng, np.float64, max_dims=5)
+        got, want = run_gpu(c), run_oracle(c)
+        assert np.array_equal(got, want), (trial, c["level"], c["dim"])
+
+
 @pytest.mark.parametrize("wavelet", ["hat", "biorthogonal", "fullweighting"])
 def test_full_outputs_equal_full_transform(wavelet):
     """Outputs = the whole grid: the restricted transform is transform_in."""
@@ -187,6 +196,14 @@ def test_errors():
                                         device="cuda"), 0, (3,), (4,),
                             [3], filters, ((0,), (1,), (2,)),
                             window_front=(1,))
+    # Compensated FP32 is not available for restricted outputs.
+    lib = _lib.load()
+    rc = lib.paliwa_gb_transform_outputs(
+        g.data_ptr(), _lib.F32C, 1, _lib.i64(level), _lib.i64(maximum),
+        _lib.i64([0]), _lib.i64([8]), 0, _lib.i64([4]), 1, _lib.i32([1]),
+        _lib.f64([-0.5, 1.0, -0.5]), 1, _lib.i64([0]), _lib.i64([1]),
+        _lib.i64([1]), None)
+    assert rc == _lib.INVALID_ARGUMENT
     # Empty outputs return at once, whatever the window.
     T.transform_outputs(g, 0, level, maximum, [4, 3, 2, 1], filters,
                         ((4,), (0,), (1,)))

@@ -332,7 +332,7 @@ def run_reference(args, w, world, rank):
 DRAM_RATIO_FILE = "profiles/lift_kernels_4d_ct_20_dram_ratio.txt"
 # Groups of grids whose host copies overlap each other's transforms in the
 # end-to-end measurement.
-E2E_GROUPS = 16
+E2E_GROUPS = 32
 E2E_COPY_STREAMS = 1
 
 

@@ -91,6 +91,40 @@ int main() {
       paliwa::pole_pass_segments({0, 0}, 0, std::numeric_limits<int>::digits,
                                  std::numeric_limits<int>::digits, 1);
     }));
+    // pole_pass_segments against explicit slot arithmetic for every level,
+    // pass, origin, parity, start and count on small pencils
+    // (test/test_paliwa_plan.cpp:355-401).
+    for (int level = 1; level <= 5; ++level) {
+      int const period = 1 << level;
+      long const spacing = 4;
+      for (int pass = 1; pass <= level; ++pass) {
+        int const dist = 1 << (level - pass);
+        for (int origin = 0; origin < period; ++origin)
+          for (int parity = 0; parity < 2; ++parity)
+            for (int start = parity * dist; start < period; start += 2 * dist)
+              for (int count = 1; count <= period / (2 * dist); ++count) {
+                int const last = (start + (count - 1) * 2 * dist) % period;
+                auto const parts = paliwa::pole_pass_segments(
+                    {start * spacing, last * spacing},
+                    static_cast<std::size_t>(origin * spacing), level,
+                    level + 2, pass);
+                std::vector<std::array<int, 3>> got, want;
+                for (auto const &r : parts)
+                  for (int k = 0; k < r.count; ++k)
+                    got.push_back({r.first + k * r.stride,
+                                   r.lower + k * r.stride,
+                                   r.upper + k * r.stride});
+                auto slot = [&](int x) {
+                  return (x - origin + 2 * period) % period;
+                };
+                for (int i = 0; i < count; ++i) {
+                  int const x = (start + i * 2 * dist) % period;
+                  want.push_back({slot(x), slot(x - dist), slot(x + dist)});
+                }
+                EXPECT(got == want);
+              }
+      }
+    }
     // for_each_transform_index visits every uid of the planned bounds once
     // (paliwa_domains.hpp:454-469): outputs 4..7 of a 16-point hat
     // hierarchization need uids 0 and 4..8.

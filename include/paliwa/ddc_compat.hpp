@@ -63,6 +63,9 @@ template <class... Tags> struct DiscreteElement {
   template <class T> constexpr long uid() const {
     return uid_[detail::index_of<T, Tags...>()];
   }
+  template <class T> constexpr long &uid() {
+    return uid_[detail::index_of<T, Tags...>()];
+  }
   constexpr bool operator==(DiscreteElement const &o) const {
     return uid_ == o.uid_;
   }

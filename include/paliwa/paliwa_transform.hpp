@@ -8,6 +8,7 @@
 //   transform_in<Dim> (full-grid overload)               (:215-251)
 //   transform_in<Dim> (restricted outputs)               (:258-344)
 //   for_each_transform_index<Dim>            (paliwa_domains.hpp:454-469)
+//   restrict_periodic_bounds<Dim>            (paliwa_domains.hpp:540-567)
 //   transform_bounds, covering_periodic_bounds, pole_pass_segments
 //                                  (paliwa_plan.hpp, paliwa_domains.hpp)
 //   strided_domain_from_level                (paliwa_domains.hpp:33-49)
@@ -270,6 +271,40 @@ void for_each_transform_index(std::vector<PeriodicBounds> const &bounds,
     for (long x = b.min; x <= last; x += stride)
       visit(ddc::DiscreteElement<Dim>(x % period));
   }
+}
+
+// paliwa_domains.hpp:540-567: the points of `domain` whose uid along Dim
+// lies in the periodic bounds, as at most two strided domains (a wrapped
+// interval splits at the period); the lattice of `domain` is kept.
+template <typename Dim, typename... Dims>
+std::vector<ddc::StridedDiscreteDomain<Dims...>>
+restrict_periodic_bounds(ddc::StridedDiscreteDomain<Dims...> const &domain,
+                         PeriodicBounds bounds, long period) {
+  std::vector<ddc::StridedDiscreteDomain<Dims...>> parts;
+  if (bounds.empty() || domain.size() == 0) return parts;
+  long const first = static_cast<long>(domain.front().template uid<Dim>());
+  long const stride = static_cast<long>(domain.strides().template get<Dim>());
+  long const last =
+      first + (static_cast<long>(domain.extents().template get<Dim>()) - 1) *
+                  stride;
+  auto add = [&](long lo, long hi) {
+    lo = std::max(lo, first);
+    hi = std::min(hi, last);
+    long const begin = first + ((lo - first + stride - 1) / stride) * stride;
+    if (begin > hi) return;
+    auto f = domain.front();
+    f.template uid<Dim>() = begin;
+    auto e = domain.extents();
+    e.template get<Dim>() = (hi - begin) / stride + 1;
+    parts.emplace_back(f, e, domain.strides());
+  };
+  if (bounds.min <= bounds.max) {
+    add(bounds.min, bounds.max);
+  } else {
+    add(bounds.min, period - 1);
+    add(0, bounds.max);
+  }
+  return parts;
 }
 
 // Restricted-output transform (paliwa_transform.hpp:333-344): the lifting

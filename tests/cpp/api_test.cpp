@@ -125,6 +125,24 @@ int main() {
               }
       }
     }
+    // restrict_periodic_bounds: the odd lattice of a 64-point axis (stride
+    // 2 from uid 1) inside [60, 5] wrapped: {61, 63} and {1, 3, 5}.
+    {
+      using V2 = ddc::DiscreteVector<X, Y>;
+      ddc::StridedDiscreteDomain<X, Y> const odd(
+          ddc::DiscreteElement<X, Y>(std::array<long, 2>{1, 0}), V2(32, 4),
+          V2(2, 1));
+      auto const parts =
+          paliwa::restrict_periodic_bounds<X>(odd, {60, 5}, 64);
+      EXPECT(parts.size() == 2);
+      EXPECT(parts[0].front().uid<X>() == 61 &&
+             parts[0].extents().get<X>() == 2);
+      EXPECT(parts[1].front().uid<X>() == 1 &&
+             parts[1].extents().get<X>() == 3);
+      EXPECT(parts[0].extents().get<Y>() == 4 &&
+             parts[0].strides().get<X>() == 2);
+      EXPECT(paliwa::restrict_periodic_bounds<X>(odd, {}, 64).empty());
+    }
     // for_each_transform_index visits every uid of the planned bounds once
     // (paliwa_domains.hpp:454-469): outputs 4..7 of a 16-point hat
     // hierarchization need uids 0 and 4..8.

@@ -327,3 +327,42 @@ def test_missing_input_is_an_error():
     with pytest.raises(RuntimeError):
         R.transform_outputs(buf, front, c["level"], c["maximum"], 0,
                             c["levels"], FIVE_PASSES, *c["outputs"])
+
+
+def test_library_argument_errors_without_gpu():
+    """paliwa_gb_transform_outputs validates everything on the host before
+    any launch: shapes and levels (std::invalid_argument), a required input
+    outside the window (std::runtime_error, paliwa_transform.hpp:282-289),
+    and returns at once for empty outputs. The grid pointer is never
+    dereferenced on these paths."""
+    lib = _lib.load()
+    fake = 256  # an aligned address that is never touched here
+    hat = [(1, (-0.5, 1.0, -0.5))]
+
+    def call(dtype=_lib.F64, level=(4,), maximum=(4,), front=(0,),
+             extents=(16,), levels=(4, 3, 2, 1), filters=hat,
+             outputs=((4,), (4,), (1,)), grid=fake):
+        of, oe, os_ = outputs
+        return lib.paliwa_gb_transform_outputs(
+            grid, dtype, len(level), _lib.i64(level), _lib.i64(maximum),
+            _lib.i64(front), _lib.i64(extents), 0, _lib.i64(levels),
+            len(levels), _lib.i32([o for o, _ in filters]),
+            _lib.f64([c for _, f in filters for c in f]), len(filters),
+            _lib.i64(of), _lib.i64(oe), _lib.i64(os_), None)
+
+    assert call(outputs=((4,), (0,), (1,)), grid=None) == _lib.OK
+    assert call(dtype=_lib.F32C) == _lib.INVALID_ARGUMENT
+    assert call(grid=None) == _lib.INVALID_ARGUMENT
+    assert call(extents=(17,)) == _lib.INVALID_ARGUMENT
+    assert call(level=(3,), maximum=(4,), front=(1,), extents=(8,),
+                levels=(3, 2, 1), outputs=((2,), (1,), (2,))) == \
+        _lib.INVALID_ARGUMENT  # front off the level-3 lattice
+    assert call(levels=(4, 2)) == _lib.INVALID_ARGUMENT  # not consecutive
+    assert call(filters=[(2, (0.0, 1.0, 0.0))]) == _lib.INVALID_ARGUMENT
+    # Outputs 4..7 need inputs around the whole axis; the window holds
+    # uids 0..7 only.
+    assert call(extents=(8,)) == _lib.RUNTIME_ERROR
+    assert b"missing required input" in lib.paliwa_gb_last_error()
+    # A second dimension whose outputs leave the window.
+    assert call(level=(4, 2), maximum=(4, 2), front=(0, 0), extents=(16, 2),
+                outputs=((4, 0), (4, 4), (1, 1))) == _lib.INVALID_ARGUMENT

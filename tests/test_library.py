@@ -74,3 +74,15 @@ def test_argument_errors_without_gpu():
     rc = lib.paliwa_gb_hierarchize(None, 9, 2, lv, _lib.i64([0, 0]), lv, 0,
                                    None)
     assert rc == _lib.INVALID_ARGUMENT
+
+
+def test_batch_and_ct_null_handles_without_gpu():
+    """Entry points taking a handle reject a null one before any CUDA call."""
+    lib = _lib.load()
+    assert lib.paliwa_gb_batch_set_groups(None, 2) == _lib.INVALID_ARGUMENT
+    assert lib.paliwa_gb_batch_hierarchize(None, None) == \
+        _lib.INVALID_ARGUMENT
+    assert lib.paliwa_gb_ct_combine(None, None, None) == \
+        _lib.INVALID_ARGUMENT
+    lib.paliwa_gb_batch_destroy(None)  # no-op
+    lib.paliwa_gb_ct_destroy(None)

@@ -207,3 +207,68 @@ def test_errors():
     # Empty outputs return at once, whatever the window.
     T.transform_outputs(g, 0, level, maximum, [4, 3, 2, 1], filters,
                         ((4,), (0,), (1,)))
+
+
+@pytest.mark.parametrize("wavelet", ["hat", "biorthogonal", "fullweighting"])
+@pytest.mark.parametrize("slabs", [2, 4])
+def test_slab_decomposition_equals_serial(wavelet, slabs):
+    """The single-GPU form of the reference's distributed-vs-serial tests
+    (test/test_paliwa_distributed.cpp:240-273, 455-461): the grid is cut
+    into `slabs` slabs along each axis in turn; every slab is transformed on
+    its own in a window buffer holding it and its periodic halo (what the
+    reference exchanges between ranks), and the slabs' outputs, put back
+    together after each axis, equal the serial hierarchize (and, after the
+    inverse, dehierarchize) bit for bit."""
+    import torch
+    level, lmin, maximum = (6, 5, 4), (1, 0, 2), (6, 5, 4)
+    rng = np.random.default_rng(slabs)
+    x = rng.uniform(-1, 1, [1 << l for l in level])
+    for forward in (True, False):
+        table = oracle.FORWARD if forward else oracle.INVERSE
+        filters = table[wavelet]
+        want = x.copy()
+        oracle.hierarchize(want, level, lmin, maximum, wavelet,
+                           forward=forward)
+        state = x.copy()
+        for dim in range(3):
+            n = 1 << level[dim]
+            levels = list(range(lmin[dim] + 1, level[dim] + 1))
+            if forward:
+                levels.reverse()
+            if not levels:
+                continue
+            out = state.copy()
+            size = n // slabs
+            for sl in range(slabs):
+                start = sl * size
+                bounds = R.transform_bounds(
+                    (start, start + size - 1), level[dim], maximum[dim],
+                    levels, filters)
+                need = sorted(set(R.transform_indices(bounds, maximum[dim])) |
+                              set(range(start, start + size)))
+                cov = R.covering_periodic_bounds(need, n)
+                ext = (cov[1] - cov[0]) % n + 1
+                idx = (cov[0] + np.arange(ext)) % n
+                buf = np.ascontiguousarray(np.take(state, idx, axis=dim))
+                g = torch.from_numpy(buf).cuda()
+                front = [0, 0, 0]
+                front[dim] = cov[0]
+                ofront = [0, 0, 0]
+                ofront[dim] = start
+                oext = [1 << l for l in level]
+                oext[dim] = size
+                T.transform_outputs(g, dim, level, maximum, levels, filters,
+                                    (ofront, oext, (1, 1, 1)),
+                                    window_front=front)
+                torch.cuda.synchronize()
+                res = g.cpu().numpy()
+                for k in range(size):
+                    j = (start + k - cov[0]) % n
+                    dst = [slice(None)] * 3
+                    src = [slice(None)] * 3
+                    dst[dim] = start + k
+                    src[dim] = j
+                    out[tuple(dst)] = res[tuple(src)]
+            state = out
+        assert np.array_equal(state, want), (wavelet, slabs, forward)
+        x = want if forward else x

@@ -171,18 +171,20 @@ int paliwa_gb_dump_to_binary_file(const void *data, int64_t bytes,
 /* The transform of paliwa_gb_hierarchize (direction 1) or
  * paliwa_gb_dehierarchize (direction -1) without any device allocation.
  * No counterpart in the reference: it is for callers that cannot let a
- * library allocate device memory -- code being captured into a CUDA graph
- * that must replay without allocation nodes, applications whose own
- * allocator already holds the device memory, solver loops that cannot afford
- * allocator latency or cudaFree's device synchronization.
+ * library allocate device memory -- programs whose own allocator already
+ * holds the GPU's memory (a framework's caching pool, a solver's arena),
+ * where a library allocation can fail or fragment it, and time-step loops
+ * that cannot pay for allocator calls or cudaFree's device synchronization.
  * Only grids with a pencil longer than 4096 points need scratch; this entry
  * point takes it from one 64 MiB array in device memory that every GPU
  * loading the library holds until the process exits, so such grids may be at
  * most 64 MiB (larger ones return PALIWA_GB_INVALID_ARGUMENT before any work
  * is queued). The first call on each device looks up that array's address
  * (cudaGetSymbolAddress) with the device current; make it before any stream
- * capture. All calls share the array: calls whose work overlaps on the GPU
- * (different streams) race on it and must be ordered by the caller. */
+ * capture. All calls share the array, which keeps the last call's contents
+ * (the transform writes every byte it reads back, so nothing is cleared):
+ * calls whose work overlaps on the GPU (different streams) race on it and
+ * must be ordered by the caller. */
 int paliwa_gb_transform_noalloc(void *grid, int dtype, int ndim,
                                 const int64_t *level,
                                 const int64_t *minimum_level,

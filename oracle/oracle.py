@@ -245,3 +245,94 @@ def scatter(subspace_values, subspaces, maximum_level):
     for v, s in zip(subspace_values, subspaces):
         full[subspace_slices(s, maximum_level)] += v
     return full
+
+
+# --------------------------------------------------------------------------
+# The same combine and restriction, vectorised per grid, for full-size
+# schemes (thousands of grids): every point of a grid at level lv belongs to
+# exactly one hierarchical subspace s <= lv; along an axis, compact index
+# i > 0 lies in s = lv - ctz(i) at position i >> (lv - s + 1), and i = 0 in
+# s = 0. The sparse grid is laid out as the library lays it out: the kept
+# subspaces in lexicographic order, each dense over the extents of
+# strided_hierarchical_domain_from_level(s, L) (paliwa_domains.hpp:51-83),
+# concatenated.
+
+
+def sparse_offsets(subspaces):
+    """First sparse point of each subspace (in the given order) and the total."""
+    offsets, total = {}, 0
+    for s in subspaces:
+        offsets[tuple(s)] = total
+        total += subspace_size(s)
+    return offsets, total
+
+
+def _axis_subspace(l):
+    i = np.arange(1 << l, dtype=np.int64)
+    s = np.zeros_like(i)
+    pos = np.zeros_like(i)
+    nz = i > 0
+    ctz = np.zeros_like(i)
+    v = i[nz]
+    c = np.zeros_like(v)
+    while True:
+        odd = (v & 1) == 1
+        if odd.all():
+            break
+        c += ~odd
+        v = np.where(odd, v, v >> 1)
+    ctz[nz] = c
+    s[nz] = l - ctz[nz]
+    pos[nz] = i[nz] >> (l - s[nz] + 1)
+    ext = np.where(s == 0, 1, 1 << np.maximum(s - 1, 0))
+    return s, pos, ext
+
+
+def grid_sparse_index(lv, offsets):
+    """Sparse index of every point of a grid at level ``lv`` (row-major,
+    int64), -1 where the point's subspace is not kept."""
+    d = len(lv)
+    axes = [_axis_subspace(int(l)) for l in lv]
+    shape = [1 << int(l) for l in lv]
+    # Local subspace table: multi-index s (0 <= s_k <= lv_k) -> offset or -1.
+    dims = [int(l) + 1 for l in lv]
+    table = np.full(math.prod(dims), -1, dtype=np.int64)
+    for flat, s in enumerate(itertools.product(*[range(n) for n in dims])):
+        table[flat] = offsets.get(s, -1)
+    def bcast(a, k):
+        sh = [1] * d
+        sh[k] = a.shape[0]
+        return a.reshape(sh)
+    local = np.zeros(shape, dtype=np.int64)
+    for k in range(d):
+        local = local * dims[k] + bcast(axes[k][0], k)
+    base = table[local]
+    inner = np.zeros(shape, dtype=np.int64)
+    stride = np.ones(shape, dtype=np.int64)
+    for k in reversed(range(d)):
+        inner = inner + bcast(axes[k][1], k) * stride
+        stride = stride * bcast(axes[k][2], k)
+    return np.where(base >= 0, base + inner, -1)
+
+
+def combine_sparse(grids, all_levels, coefficients, offsets, total):
+    """test_paliwa_combination_technique.cpp:256-290, as one flat float64
+    vector: grids in order, sparse += coefficient * grid on every kept point
+    (the product rounded, then the sum, as ``acc += c * g``)."""
+    sparse = np.zeros(total)
+    for g, lv, c in zip(grids, all_levels, coefficients):
+        idx = grid_sparse_index(lv, offsets).ravel()
+        keep = idx >= 0
+        sparse[idx[keep]] += float(c) * np.asarray(g, np.float64).ravel()[keep]
+    return sparse
+
+
+def restrict_sparse(grid, lv, sparse, offsets):
+    """The restriction of the combined sparse grid back into one component
+    grid: every kept point takes the combined value (rounded to the grid's
+    storage type); the other points are left as they are."""
+    idx = grid_sparse_index(lv, offsets).ravel()
+    keep = idx >= 0
+    flat = grid.reshape(-1)
+    flat[keep] = sparse[idx[keep]].astype(grid.dtype)
+    return grid

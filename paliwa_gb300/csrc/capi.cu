@@ -410,9 +410,15 @@ void plan_axis(AxisView const &view, std::vector<int> const &shifts,
   }
 }
 
-int device_sms() {
-  int dev = 0, sms = 0;
+int current_device() {
+  int dev = 0;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  return dev;
+}
+
+int device_sms() {
+  int const dev = current_device();
+  int sms = 0;
   cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
              "cudaDeviceGetAttribute");
   return sms;
@@ -652,9 +658,8 @@ int paliwa_gb_dehierarchize(void *grid, int dtype, int ndim,
 namespace pgb {
 
 void launch_copy(LiftParams const &p, cudaStream_t s) {
-  static thread_local int per_sm = 0;
-  static thread_local int sms = 0;
-  launch_persistent(copy_kernel<kThreads>, 0, p, s, per_sm, sms);
+  static thread_local Occupancy occ;
+  launch_persistent(copy_kernel<kThreads>, 0, p, s, occ);
 }
 
 } // namespace pgb

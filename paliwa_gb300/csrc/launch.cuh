@@ -12,24 +12,40 @@
 namespace pgb {
 
 int device_sms();
+int current_device();
 
-// One persistent launch: as many CTAs as fit on the device at once, or one
-// per tile when there are fewer tiles. `per_sm` and `sms` cache the
-// occupancy of this kernel (one pair per kernel instantiation).
+// Occupancy of one kernel instantiation, per device: the dynamic shared
+// memory opt-in (cudaFuncSetAttribute) and the occupancy query apply to the
+// device that is current when they are made, so a host thread that drives
+// several GPUs needs one entry per device ordinal.
+struct Occupancy {
+  static constexpr int kMaxDevices = 64;
+  int per_sm[kMaxDevices] = {};
+  int sms[kMaxDevices] = {};
+};
+
+// One persistent launch on the current device: as many CTAs as fit on it at
+// once, or one per tile when there are fewer tiles.
 template <typename Kernel>
 void launch_persistent(Kernel kernel, size_t smem, LiftParams const &p,
-                       cudaStream_t s, int &per_sm, int &sms) {
+                       cudaStream_t s, Occupancy &occ) {
+  int const dev = current_device();
+  if (dev < 0 || dev >= Occupancy::kMaxDevices)
+    throw StatusError(2, "device ordinal beyond the launch cache");
+  int &per_sm = occ.per_sm[dev];
+  int &sms = occ.sms[dev];
   if (per_sm == 0) {
     if (smem > 0)
       cuda_check(cudaFuncSetAttribute(
                      kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                      static_cast<int>(smem)),
                  "cudaFuncSetAttribute");
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &per_sm, kernel, kThreads, smem),
+    int n = 0;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel,
+                                                             kThreads, smem),
                "occupancy query");
     sms = device_sms();
-    if (per_sm < 1) per_sm = 1;
+    per_sm = n < 1 ? 1 : n;
   }
   long long const resident = static_cast<long long>(per_sm) * sms;
   long long const blocks = std::min(p.total_tiles, resident);
@@ -41,27 +57,23 @@ template <class A, int R, class Sched, bool Direct>
 void launch_r(LiftParams const &p, cudaStream_t s) {
   // Direct kernels keep pencils in registers and need no staging memory.
   size_t const smem = Direct ? 0 : lift_smem_bytes<A, R, kThreads>(kRounds);
-  static thread_local int per_sm = 0;
-  static thread_local int sms = 0;
+  static thread_local Occupancy occ;
   launch_persistent(lift_kernel<A, R, kThreads, Sched, Direct>, smem, p, s,
-                    per_sm, sms);
+                    occ);
 }
 
 template <class A, int R, class Sched, bool Contig>
 void launch_wide_r(LiftParams const &p, cudaStream_t s) {
-  static thread_local int per_sm = 0;
-  static thread_local int sms = 0;
+  static thread_local Occupancy occ;
   launch_persistent(wide_kernel<A, R, kThreads, Sched, Contig>,
-                    wide_smem_bytes<A, R, kThreads>(), p, s, per_sm, sms);
+                    wide_smem_bytes<A, R, kThreads>(), p, s, occ);
 }
 
 template <class A, int R, class Sched, bool Long>
 void launch_tile_r(LiftParams const &p, cudaStream_t s) {
-  static thread_local int per_sm = 0;
-  static thread_local int sms = 0;
+  static thread_local Occupancy occ;
   launch_persistent(tile_kernel<A, R, kThreads, Sched, Long>,
-                    tile_smem_bytes<A, R, kThreads, Long>(), p, s, per_sm,
-                    sms);
+                    tile_smem_bytes<A, R, kThreads, Long>(), p, s, occ);
 }
 
 // Row policy A (arith.cuh), code kWide + R (strided axis) or kWideContig + R

@@ -1,10 +1,9 @@
 // Allocation-free single-grid transform (paliwa_gb_transform_noalloc).
 //
-// Some callers cannot let a library allocate device memory: code that is
-// being captured into a CUDA graph that must replay without allocation
-// nodes, applications whose framework allocator has already reserved the
-// device memory (a driver allocation would fail or fragment it), and
-// per-timestep solver loops that cannot afford allocator latency or the
+// Some callers cannot let a library allocate device memory: programs whose
+// own allocator already holds the GPU's memory (a framework's caching pool,
+// a solver's arena), where a driver allocation can fail or fragment that
+// memory, and time-step loops that cannot pay for allocator calls or for the
 // device synchronization that cudaFree implies. paliwa_gb_hierarchize needs
 // scratch only for grids with a pencil longer than 4096 points (the shadow
 // buffer of its windowed stages) and takes it from the stream-ordered
@@ -33,7 +32,8 @@ std::mutex g_scratch_mutex;
 std::array<void *, 256> g_scratch_address{};  // by device ordinal
 
 // Host code may not use g_scratch's name as an address: the device address
-// is looked up once per device, with that device current.
+// is looked up once per device, with that device current, by the first call
+// on that device (so that call should come before any stream capture).
 void *scratch_address() {
   int dev = 0;
   pgb::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");

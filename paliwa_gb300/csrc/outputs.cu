@@ -99,7 +99,13 @@ int device_sm_count() {
 }
 
 void launch_out_pass(int dtype, bool exact, OutPass const &p, cudaStream_t s) {
-  static thread_local int sms = 0;
+  // SM count of the current device (a thread may drive several GPUs).
+  static thread_local int sms_by_device[64] = {};
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= 64)
+    throw StatusError(PALIWA_GB_RUNTIME_ERROR, "device ordinal too large");
+  int &sms = sms_by_device[dev];
   if (sms == 0) sms = device_sm_count();
   // Enough CTAs for 8 per SM (the kernel is latency-bound on three
   // scattered loads per thread); larger passes loop.

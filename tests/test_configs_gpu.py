@@ -4,9 +4,14 @@ C1 (2D hat, 64 x 64, the reference's CPU-sized case) and C2 (3D CDF
 biorthogonal, 512^3) and C3 (6D hat, 32^4 x 16^2) are compared with the CPU
 oracle point for point in FP64 (bit-identical), forward and inverse, on the
 bench's seeded inputs; FP32c is held to the normwise 1e-6 target on C3. C4
-(the batched 4D combination technique, 3,025 grids, 1.7 G points) is checked
-through size-independent properties: the FP64 round trip, and the FP32c
-forward against the FP64 forward within the target.
+(the batched 4D combination technique, 3,025 grids, 1.7 G points) is
+compared with the oracle grid by grid in FP64, forward and inverse
+(bit-identical), and checked through size-independent properties: the FP64
+round trip, exact linearity, and the FP32c forward against the FP64 forward
+within the target. C5 (the 6D scheme, 7,798 grids) runs its whole FP64
+pipeline -- forward, combine, restrict, inverse -- against the oracle's
+restatement of the reference driver (bit-identical at every stage), and its
+FP32c pipeline against the FP64 one per q.
 """
 import math
 
@@ -190,3 +195,96 @@ def test_c5_ct_pipeline_per_q_error():
     assert rel <= 1e-6, rel
     for h in (ct64, ct32, bt64, bt32):
         h.close()
+
+
+def test_c4_fp64_full_size_bit_exact_against_oracle():
+    """C4 at full size (3,025 grids, 1.7 G points) in FP64: the batched
+    forward and inverse transforms of every grid are bit-identical to the
+    CPU oracle's hierarchize and dehierarchize of the same grid."""
+    import torch
+    import bench
+    from paliwa_gb300 import ct as pct
+    O = oracle()
+    w = bench.Workload("4d-ct-20")
+    b64, v64 = pct.packed_grids(w.levels, torch.float64)
+    for i, v in enumerate(v64):
+        v.copy_(torch.from_numpy(np.ascontiguousarray(
+            w.grid_values(i)).reshape(-1)))
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    bt = pct.Batch(v64, w.levels, w.lmin, w.lmax, w.wavelet)
+
+    def expected(i, forward):
+        x = np.ascontiguousarray(w.grid_values(i))
+        y = O.hierarchize(x, w.levels[i], w.lmin, w.lmax, w.wavelet)
+        if not forward:
+            y = O.dehierarchize(y, w.levels[i], w.lmin, w.lmax, w.wavelet)
+        return y
+
+    for forward in (True, False):
+        (bt.hierarchize if forward else bt.dehierarchize)(s)
+        s.synchronize()
+        host = b64.cpu().numpy()
+        starts = [(v.data_ptr() - b64.data_ptr()) // 8 for v in v64]
+        bad = [i for i, lv in enumerate(w.levels) if not np.array_equal(
+            host[starts[i]:starts[i] + (1 << sum(lv))],
+            expected(i, forward).reshape(-1))]
+        assert not bad, (forward, len(bad), bad[:5])
+    bt.close()
+
+
+def test_c5_fp64_pipeline_bit_exact_against_oracle():
+    """C5 at full size (6D, 7,798 grids) in FP64: forward transform of every
+    grid, combine into the kept sparse-grid subspaces, restrict back into the
+    grids, inverse transform -- each stage bit-identical to the oracle's
+    restatement of the reference driver (hierarchize per grid,
+    test/test_paliwa_combination_technique.cpp:256-290 for the combine)."""
+    import torch
+    import bench
+    from paliwa_gb300 import ct as pct
+    O = oracle()
+    w = bench.Workload("6d-ct-16")
+    b64, v64 = pct.packed_grids(w.levels, torch.float64)
+    inputs = [np.ascontiguousarray(w.grid_values(i)) for i in
+              range(len(w.levels))]
+    for v, x in zip(v64, inputs):
+        v.copy_(torch.from_numpy(x.reshape(-1)))
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    bt = pct.Batch(v64, w.levels, w.lmin, w.lmax, w.wavelet)
+    ct = pct.CombinationTechnique(v64, w.levels, w.coeffs, w.lmax)
+    starts = [(v.data_ptr() - b64.data_ptr()) // 8 for v in v64]
+
+    def grids_of(host):
+        return [host[a:a + (1 << sum(lv))].reshape([1 << l for l in lv])
+                for a, lv in zip(starts, w.levels)]
+
+    bt.hierarchize(s)
+    s.synchronize()
+    want = [O.hierarchize(x.copy(), lv, w.lmin, w.lmax, w.wavelet)
+            for x, lv in zip(inputs, w.levels)]
+    got = grids_of(b64.cpu().numpy())
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
+
+    sparse = ct.combine(stream=s)
+    s.synchronize()
+    subs, offs_lib = ct.subspaces()
+    assert subs == O.kept_subspaces(w.levels)
+    offs, total = O.sparse_offsets(subs)
+    assert total == ct.npoints
+    assert [offs[sb] for sb in subs] == offs_lib
+    want_sparse = O.combine_sparse(want, w.levels, w.coeffs, offs, total)
+    assert np.array_equal(sparse.cpu().numpy(), want_sparse)
+
+    ct.restrict(sparse, stream=s)
+    bt.dehierarchize(s)
+    s.synchronize()
+    for g, lv in zip(want, w.levels):
+        O.restrict_sparse(g, lv, want_sparse, offs)
+        O.dehierarchize(g, lv, w.lmin, w.lmax, w.wavelet)
+    got = grids_of(b64.cpu().numpy())
+    bad = [i for i, (a, b) in enumerate(zip(got, want))
+           if not np.array_equal(a, b)]
+    assert not bad, (len(bad), bad[:5])
+    ct.close()
+    bt.close()

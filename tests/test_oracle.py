@@ -149,3 +149,32 @@ def test_c1_configuration_round_trip(oracle_mod):
     assert h[0, 0] == f[0, 0]
     back = oracle_mod.dehierarchize(h, (6, 6), (0, 0), (6, 6), "hat")
     assert np.max(np.abs(back - f)) <= 1e-13 * np.max(np.abs(f))
+
+
+def test_vectorised_combine_and_restrict_match_the_driver_restatement():
+    """The per-grid vectorised combine (used for full-size schemes) equals the
+    subspace-by-subspace restatement of the reference driver
+    (test/test_paliwa_combination_technique.cpp:256-290) bit for bit, and
+    the restriction writes exactly the kept points."""
+    import itertools
+    import oracle as O
+    for d, top in ((2, 9), (3, 7), (4, 7)):
+        levels = [l for q in range(d) for l in itertools.product(
+            range(1, top + 1), repeat=d) if sum(l) == top - q]
+        coeffs = [(-1) ** (top - sum(l)) * math.comb(d - 1, top - sum(l))
+                  for l in levels]
+        rng = np.random.default_rng(d)
+        grids = [rng.standard_normal([1 << x for x in l]) for l in levels]
+        subs = O.kept_subspaces(levels)
+        slow = O.combine(grids, levels, coeffs, None, subs)
+        offs, total = O.sparse_offsets(subs)
+        fast = O.combine_sparse(grids, levels, coeffs, offs, total)
+        assert np.array_equal(np.concatenate([a.ravel() for a in slow]), fast)
+        for g, lv in zip(grids[:5], levels[:5]):
+            r = O.restrict_sparse(g.copy(), lv, fast, offs)
+            for s, v in zip(subs, slow):
+                if all(si <= li for si, li in zip(s, lv)):
+                    assert np.array_equal(r[O.subspace_slices(s, lv)], v)
+            changed = r != g
+            idx = O.grid_sparse_index(lv, offs)
+            assert not changed[idx < 0].any()

@@ -56,6 +56,7 @@ def lib():
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_transform_in.restype = ctypes.c_int
         L.oracle_hierarchize.restype = ctypes.c_int
+        L.oracle_transform_in_window.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -101,6 +102,24 @@ def transform_in(grid, level, maximum_level, dim, levels, filters, mode=0):
         grid.ctypes.data_as(ctypes.c_void_p), _dtype_code(grid), len(level),
         _longs(level), _longs(maximum_level), int(dim), _longs(levels or [0]),
         len(levels), offs, co, len(filters), int(mode)))
+    return grid
+
+
+def transform_in_window(grid, level, maximum_level, front, dim, levels,
+                        filters):
+    """transform_in along ``dim`` on a chunk holding the window of the level
+    lattice whose front uids are ``front`` and whose extents are
+    ``grid.shape`` (the reference's checked lifting passes,
+    paliwa_transform.hpp:24-51 with CheckBounds, :224-247)."""
+    assert grid.flags.c_contiguous
+    offs = (ctypes.c_int * max(1, len(filters)))(*[int(o) for o, _ in filters])
+    co = (ctypes.c_double * max(1, 3 * len(filters)))(
+        *[float(c) for _, f in filters for c in f])
+    _check(lib().oracle_transform_in_window(
+        grid.ctypes.data_as(ctypes.c_void_p), _dtype_code(grid), len(level),
+        _longs(level), _longs(maximum_level), _longs(front),
+        _longs(grid.shape), int(dim), _longs(levels or [0]), len(levels),
+        offs, co, len(filters)))
     return grid
 
 

@@ -90,6 +90,32 @@ int oracle_transform_in(void *grid, int dtype, int ndim, long const *level,
   });
 }
 
+// transform_in over one dimension of a chunk holding a window of the level
+// lattice (front uids, extents): the reference's checked lifting passes.
+int oracle_transform_in_window(void *grid, int dtype, int ndim,
+                               long const *level, long const *maximum_level,
+                               long const *front, long const *extents, int dim,
+                               long const *levels, int nlevels,
+                               int const *offsets, double const *coeffs,
+                               int npasses) {
+  return guarded([&] {
+    auto const shape = make_shape(ndim, level, maximum_level);
+    if (dim < 0 || dim >= ndim) throw std::invalid_argument("bad dim");
+    for (int d = 0; d < ndim; ++d)
+      if (extents[d] < 0 || front[d] < 0 ||
+          front[d] % (1L << (maximum_level[d] - level[d])) != 0)
+        throw std::invalid_argument("window off the level lattice");
+    std::vector<long> lv(levels, levels + nlevels);
+    auto const filters = make_filters(offsets, coeffs, npasses);
+    if (dtype == 0)
+      paliwa_oracle::transform_in_window(static_cast<double *>(grid), shape,
+                                         front, extents, dim, lv, filters);
+    else
+      paliwa_oracle::transform_in_window(static_cast<float *>(grid), shape,
+                                         front, extents, dim, lv, filters);
+  });
+}
+
 // hierarchize / dehierarchize over all dimensions
 // (paliwa/paliwa_transform.hpp:401-431).
 int oracle_hierarchize(void *grid, int dtype, int ndim, long const *level,

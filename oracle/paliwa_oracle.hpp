@@ -108,6 +108,62 @@ void lifting_pass_direct(Value *g, long outer, long n, long inner, long s,
   }
 }
 
+// transform_in (full overload) on a chunk that holds only a window of the
+// level lattice: the reference's lifting_pass<CheckBounds = true>
+// (paliwa/paliwa_transform.hpp:24-51, chosen when the chunk's domain is not
+// the complete lattice, :224-228, :242-247). The window holds, along each
+// dimension d, the uids front[d] + k * 2^(L[d] - level[d]) for
+// k < extents[d] (no wrap: a DDC domain), dense and row-major. A write point
+// is updated only when it and both of its periodic neighbours (:37-41) lie
+// in the window; every other point keeps its value.
+template <typename Value>
+void transform_in_window(Value *g, Shape const &shape, long const *front,
+                         long const *extents, int dim,
+                         std::vector<long> const &levels,
+                         Filters const &filters) {
+  long outer = 1, inner = 1;
+  for (int d = 0; d < dim; ++d) outer *= extents[d];
+  for (int d = dim + 1; d < shape.ndim; ++d) inner *= extents[d];
+  long const n = extents[dim];
+  long const L = shape.maximum_level[dim];
+  long const spacing = 1L << (L - shape.level[dim]);
+  long const period = 1L << L;
+  long const f = front[dim];
+  auto index = [&](long uid) -> long {
+    long const r = uid - f;
+    if (r < 0 || r % spacing != 0) return -1;
+    return r / spacing < n ? r / spacing : -1;
+  };
+  for (long l : levels) {
+    if (l < 1 || l > shape.level[dim])
+      throw std::invalid_argument("requires 1 <= level <= grid level");
+    long const s = 1L << (L - l);
+    for (auto const &[offset, c] : filters) {
+      if (offset != 0 && offset != 1)
+        throw std::runtime_error("Filter offset not supported");
+      Value const c0 = static_cast<Value>(c[0]);
+      Value const c1 = static_cast<Value>(c[1]);
+      Value const c2 = static_cast<Value>(c[2]);
+      for (long m = 0; m < (1L << (l - 1)); ++m) {
+        long const x = offset * s + 2 * s * m;
+        long const k = index(x);
+        long const lo = index(x == 0 ? period - s : x - s);
+        long const up = index(x + s == period ? 0 : x + s);
+        if (k < 0 || lo < 0 || up < 0) continue;
+        for (long a = 0; a < outer; ++a) {
+          Value *base = g + a * n * inner;
+          for (long b = 0; b < inner; ++b) {
+            Value const vl = base[lo * inner + b];
+            Value const vm = base[k * inner + b];
+            Value const vu = base[up * inner + b];
+            base[k * inner + b] = c0 * vl + c1 * vm + c2 * vu;
+          }
+        }
+      }
+    }
+  }
+}
+
 // transform_in (full overload), paliwa/paliwa_transform.hpp:215-251: for each
 // level in the given order, for each (offset, filter) in table order, one pass.
 // `levels` are reference levels l (1 <= l <= level[dim]); the compact stride of

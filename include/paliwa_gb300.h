@@ -88,6 +88,27 @@ int paliwa_gb_transform_in(void *grid, int dtype, int ndim,
                            const int32_t *offsets, const double *coefficients,
                            int npasses, void *stream);
 
+/* Replaces paliwa::transform_in<Dim> (full-grid overload,
+ * paliwa/paliwa_transform.hpp:215-251) on a chunk that holds only a box of
+ * the level lattice, where the reference runs its bounds-checked lifting
+ * passes (lifting_pass<CheckBounds = true>, :24-51, chosen at :224-228): a
+ * point of a pass is updated only when it and both of its periodic
+ * neighbours lie in the box; every other value is left as it is. The grid
+ * holds, along dimension d, the uids window_front[d] + k * 2^(L[d] -
+ * level[d]) for k < window_extents[d] (dense, row-major; the box must not
+ * wrap around the period, like a DDC domain). F64 and F32 grids; levels
+ * 1 <= l <= level[dim]; filter offsets other than 0 and 1 return
+ * PALIWA_GB_RUNTIME_ERROR. */
+int paliwa_gb_transform_in_window(void *grid, int dtype, int ndim,
+                                  const int64_t *level,
+                                  const int64_t *maximum_level,
+                                  const int64_t *window_front,
+                                  const int64_t *window_extents, int dim,
+                                  const int64_t *levels, int nlevels,
+                                  const int32_t *offsets,
+                                  const double *coefficients, int npasses,
+                                  void *stream);
+
 /* Replaces paliwa::hierarchize_in<Dim> / dehierarchize_in<Dim>
  * (paliwa/paliwa_transform.hpp:346-399): levels level[dim] .. lmin+1
  * (forward) or lmin+1 .. level[dim] (inverse) with the wavelet's table.

@@ -19,7 +19,8 @@ from .transform import (dehierarchize, dehierarchize_in, hierarchize,
                         hierarchize_in,
                         lifting_wavelet_filter_offsets_and_coefficients,
                         lifting_wavelet_reconstruct_offsets_and_coefficients,
-                        transform_bounds, transform_in, transform_outputs,
+                        transform_bounds, transform_in, transform_in_window,
+                        transform_outputs,
                         wavelet_id)
 
 __all__ = [
@@ -32,5 +33,5 @@ __all__ = [
     "dehierarchize_in", "hierarchize", "hierarchize_in",
     "lifting_wavelet_filter_offsets_and_coefficients",
     "lifting_wavelet_reconstruct_offsets_and_coefficients", "transform_bounds",
-    "transform_in", "transform_outputs", "wavelet_id",
+    "transform_in", "transform_in_window", "transform_outputs", "wavelet_id",
 ]

@@ -39,6 +39,9 @@ SIGNATURES = {
     "paliwa_gb_wavelet_filters": (_i, [_i, _i, ctypes.POINTER(_i), _pi32, _pd]),
     "paliwa_gb_transform_in": (
         _i, [_vp, _i, _i, _pi64, _pi64, _i, _pi64, _i, _pi32, _pd, _i, _vp]),
+    "paliwa_gb_transform_in_window": (
+        _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _pi64, _i, _pi64, _i, _pi32,
+             _pd, _i, _vp]),
     "paliwa_gb_hierarchize_in": (
         _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _i, _vp]),
     "paliwa_gb_dehierarchize_in": (

@@ -374,3 +374,125 @@ int paliwa_gb_transform_outputs(
 }
 
 } // extern "C"
+
+extern "C" int paliwa_gb_transform_in_window(
+    void *grid, int dtype, int ndim, const int64_t *level,
+    const int64_t *maximum_level, const int64_t *window_front,
+    const int64_t *window_extents, int dim, const int64_t *levels,
+    int nlevels, const int32_t *offsets, const double *coefficients,
+    int npasses, void *stream) {
+  using namespace pgb;
+  return guarded([&] {
+    if (dtype != PALIWA_GB_F64 && dtype != PALIWA_GB_F32)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                        "windowed transforms support F64 and F32 grids");
+    if (ndim < 1 || ndim > kOutMaxDims)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "ndim must be in [1, 12]");
+    if (dim < 0 || dim >= ndim)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "bad dimension");
+    if (level == nullptr || maximum_level == nullptr ||
+        window_front == nullptr || window_extents == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    auto const lv = level_list(nlevels, levels);
+    auto const filters = filter_list(npasses, offsets, coefficients);
+    OutPass p{};
+    p.base = reinterpret_cast<unsigned long long>(grid);
+    p.ndim = ndim;
+    p.dim = dim;
+    long long elem = 1;
+    bool empty = false;
+    for (int d = ndim - 1; d >= 0; --d) {
+      if (level[d] < 0 || maximum_level[d] < level[d] || maximum_level[d] > 30)
+        throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                          "requires 0 <= level <= maximum_level <= 30");
+      long long const period = 1LL << maximum_level[d];
+      long long const sp = 1LL << (maximum_level[d] - level[d]);
+      long long const ext = window_extents[d];
+      // A chunk's domain: a box of the level lattice that does not wrap.
+      if (ext < 0 || window_front[d] < 0 || window_front[d] % sp != 0 ||
+          (ext > 0 && window_front[d] + (ext - 1) * sp >= period))
+        throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                          "the window must be a box of the level's lattice "
+                          "inside one period");
+      if (ext == 0) empty = true;
+      p.elem[d] = elem;
+      if (ext > 0 && elem > (1LL << 40) / ext)
+        throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "window too large");
+      elem *= ext > 0 ? ext : 1;
+      p.obase[d] = 0;
+      p.ostep[d] = 1;
+      p.oext[d] = ext;
+    }
+    long long const L = maximum_level[dim];
+    for (long l : lv)
+      if (l < 1 || l > level[dim])
+        throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                          "requires 1 <= level <= the grid's level");
+    for (auto const &f : filters)
+      if (f.first != 0 && f.first != 1)
+        throw StatusError(PALIWA_GB_RUNTIME_ERROR,
+                          "Filter offset not supported");
+    if (empty || lv.empty() || filters.empty()) return;
+    size_t const es = dtype_size(dtype);
+    if (grid == nullptr || reinterpret_cast<uintptr_t>(grid) % es != 0)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                        "grid is null or misaligned");
+    long long const period = 1LL << L;
+    long long const sp = 1LL << (L - level[dim]);
+    long long const wf = window_front[dim];
+    long long const wl = wf + (window_extents[dim] - 1) * sp;  // last uid
+    int log2_sp = 0;
+    while ((1LL << log2_sp) < sp) ++log2_sp;
+    p.log2_spacing = log2_sp;
+    p.period = period;
+    p.wfront = wf;
+    long long others = 1;
+    for (int d = 0; d < ndim; ++d)
+      if (d != dim) others *= p.oext[d];
+    bool const exact = exact_scalers([&] {
+      std::vector<Filter> v;
+      for (auto const &f : filters)
+        v.push_back({f.first, {f.second[0], f.second[1], f.second[2]}});
+      return v;
+    }());
+    cudaStream_t const s = static_cast<cudaStream_t>(stream);
+    // lifting_pass<CheckBounds = true> (paliwa_transform.hpp:24-51): a point
+    // of the pass's lattice is written when it and both periodic
+    // neighbours lie in the window. Along the axis those points are the
+    // lattice points of [wf + d, wl - d] (neighbours at distance d), plus
+    // uid 0 (lower neighbour period - d) and uid period - d (upper
+    // neighbour 0) when the window holds their wrapped neighbours; both sit
+    // at the ends of that range, so every pass writes one run.
+    for (long l : lv) {
+      long long const d = 1LL << (L - l);
+      long long const step = 2 * d;
+      p.s = d;
+      for (auto const &f : filters) {
+        long long const off = f.first * d;  // the lattice {off + k step}
+        auto up_to = [&](long long x) {      // largest lattice point <= x
+          return x - floor_mod(x - off, step);
+        };
+        auto from = [&](long long x) {       // smallest lattice point >= x
+          return x + floor_mod(off - x, step);
+        };
+        long long lo = from(wf + d), hi = up_to(wl - d);
+        auto inside = [&](long long x) { return x >= wf && x <= wl; };
+        if (off == 0 && inside(0) && inside(period - d) && inside(d))
+          lo = 0;  // uid 0 (only reached from the first point)
+        if (off + (period / step - 1) * step == period - d &&
+            inside(period - d) && inside(period - 2 * d) && inside(0))
+          hi = period - d;
+        if (hi < lo) continue;
+        p.first = lo;
+        p.step = step;
+        p.count = (hi - lo) / step + 1;
+        p.oext[dim] = p.count;
+        p.total = p.count * others;
+        double const *c = f.second.data();
+        p.c = Coeffs{c[0], c[1], c[2], static_cast<float>(c[0]),
+                     static_cast<float>(c[1]), static_cast<float>(c[2])};
+        launch_out_pass(dtype, exact, p, s);
+      }
+    }
+  });
+}

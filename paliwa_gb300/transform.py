@@ -9,7 +9,8 @@ header-only templates, over CUDA tensors instead of DDC chunk spans:
 * ``hierarchize_in(grid, dim, level, minimum_level, maximum_level, ...)``
   and ``dehierarchize_in`` -- :346-399 (``Dim`` becomes ``dim``)
 * ``transform_in(grid, dim, level, maximum_level, levels, filters)``
-  -- :215-251 (full-grid overload)
+  -- :215-251 (full-grid overload); ``transform_in_window`` for a grid that
+  holds only a box of the lattice (the reference's bounds-checked passes)
 
 A grid is a C-contiguous CUDA tensor holding the dense row-major storage of
 ``strided_domain_from_level(level, maximum_level)``: 2^level[d] points along
@@ -152,6 +153,30 @@ def transform_in(grid, dim, level, maximum_level, levels, filters,
           (_dtype_code(grid, compensated), len(level), _lib.i64(level),
            _lib.i64(maximum_level), int(dim), _lib.i64(levels), len(levels),
            _lib.i32([o for o, _ in filters]),
+           _lib.f64([c for _, f in filters for c in f]), len(filters)),
+          stream)
+    return True
+
+
+def transform_in_window(grid, dim, level, maximum_level, levels, filters,
+                        window_front, stream=None):
+    """transform_in<Dim> (full-grid overload) on a grid tensor that holds
+    only a box of the level lattice: along dimension d the uids
+    ``window_front[d] + k * 2^(maximum_level[d] - level[d])`` for
+    ``k < grid.shape[d]``. The reference's bounds-checked passes: a point is
+    updated only when it and both periodic neighbours are in the box
+    (paliwa_transform.hpp:24-51, :224-247). float64 or float32 grids."""
+    if not grid.is_contiguous():
+        raise _lib.InvalidArgument("grid must be C-contiguous")
+    if grid.dim() != len(level):
+        raise _lib.InvalidArgument("grid rank must equal len(level)")
+    filters = list(filters)
+    levels = [int(l) for l in levels]
+    code = _lib.F64 if grid.element_size() == 8 else _lib.F32
+    _call("paliwa_gb_transform_in_window", grid,
+          (code, len(level), _lib.i64(level), _lib.i64(maximum_level),
+           _lib.i64(window_front), _lib.i64(list(grid.shape)), int(dim),
+           _lib.i64(levels), len(levels), _lib.i32([o for o, _ in filters]),
            _lib.f64([c for _, f in filters for c in f]), len(filters)),
           stream)
     return True

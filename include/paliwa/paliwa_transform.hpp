@@ -7,13 +7,13 @@
 //   hierarchize_in<Dim> / dehierarchize_in<Dim>           (:346-399)
 //   transform_in<Dim> (full-grid overload)               (:215-251)
 //   transform_in<Dim> (restricted outputs)               (:258-344)
-//   for_each_transform_index<Dim>            (paliwa_domains.hpp:454-469)
-//   restrict_periodic_bounds<Dim>            (paliwa_domains.hpp:540-567)
-//   transform_bounds, covering_periodic_bounds, pole_pass_segments
-//                                  (paliwa_plan.hpp, paliwa_domains.hpp)
-//   strided_domain_from_level                (paliwa_domains.hpp:33-49)
-// Grids are ChunkSpans whose data_handle() is device memory holding the dense
-// row-major storage of strided_domain_from_level(level, maximum_level).
+//   PoleExecution                                        (:21)
+// and, through paliwa_domains.hpp, the index maps and planner of
+// paliwa/paliwa_domains.hpp. Grids are ChunkSpans whose data_handle() is
+// device memory holding the dense row-major storage of their domain: the
+// complete lattice strided_domain_from_level(level, maximum_level) runs the
+// tiled GPU transform; a chunk holding a box of that lattice runs the
+// reference's bounds-checked passes (:24-51, :224-247) on the GPU.
 // The last argument stands in for the Kokkos execution-space instance: any
 // object with a cuda_stream() member (Kokkos::Cuda has one), a
 // paliwa::gb300::Stream, or nothing (the legacy default stream). Calls are
@@ -24,6 +24,7 @@
 // (:239-240), std::out_of_range for unknown wavelet names (map::at, :370).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cstdint>
 #include <stdexcept>
@@ -39,7 +40,7 @@
 #endif
 
 #include "../paliwa_gb300.h"
-#include "paliwa_plan.hpp"
+#include "paliwa_domains.hpp"
 #include "paliwa_wavelets.hpp"
 
 namespace paliwa {
@@ -51,6 +52,8 @@ namespace gb300 {
 
 struct Stream {
   void *handle = nullptr;  // a cudaStream_t
+  // Waits for this stream's queued work, like an instance's fence().
+  void fence() const;
 };
 
 template <class T, class = void> struct has_cuda_stream : std::false_type {};
@@ -76,6 +79,8 @@ inline void check(int rc) {
   default: throw std::runtime_error(msg);
   }
 }
+
+inline void Stream::fence() const { check(paliwa_gb_synchronize(handle)); }
 
 template <class T> constexpr int dtype_of() {
   if constexpr (std::is_same_v<std::remove_cv_t<T>, double>)
@@ -107,46 +112,109 @@ template <class Dim, class... DDims> constexpr int dim_index() {
 
 } // namespace gb300
 
-// paliwa_domains.hpp:33-49: 2^l points per dimension, stride 2^(L - l).
-template <class... DDims>
-constexpr ddc::StridedDiscreteDomain<DDims...> strided_domain_from_level(
-    std::array<long int, sizeof...(DDims)> const &level,
-    std::array<long int, sizeof...(DDims)> const &finest_level,
-    ddc::DiscreteElement<DDims...> lbound = ddc::DiscreteElement<DDims...>()) {
-  std::array<long, sizeof...(DDims)> ext{}, str{};
-  for (size_t i = 0; i < sizeof...(DDims); ++i) {
-    ext[i] = 1L << level[i];
-    str[i] = 1L << (finest_level[i] - level[i]);
-  }
-  return ddc::StridedDiscreteDomain<DDims...>(
-      lbound, ddc::DiscreteVector<DDims...>(ext),
-      ddc::DiscreteVector<DDims...>(str));
-}
-
 namespace gb300 {
-// The device path transforms complete grids: the span's domain must be
-// strided_domain_from_level(level, maximum_level) (the reference's
-// "complete" case, paliwa_transform.hpp:224-228).
-template <class ChunkSpanType, class... DDims>
-void check_complete(ChunkSpanType const &grid,
-                    ddc::DiscreteVector<DDims...> const &level,
-                    ddc::DiscreteVector<DDims...> const &maximum_level) {
+
+template <class... DDims>
+void check_levels(ddc::DiscreteVector<DDims...> const &level,
+                  ddc::DiscreteVector<DDims...> const &maximum_level) {
   auto const l = levels_of(level);
   auto const L = levels_of(maximum_level);
   for (size_t i = 0; i < l.size(); ++i)
     if (l[i] < 0 || L[i] < l[i] || L[i] > 62)
       throw std::invalid_argument("requires 0 <= level <= maximum_level");
+}
+
+// Whether the span holds the complete lattice of the level
+// (paliwa_transform.hpp:224-228); those grids take the GPU's tiled
+// transforms, every other chunk the bounds-checked passes.
+template <class ChunkSpanType, class... DDims>
+bool is_complete(ChunkSpanType const &grid,
+                 ddc::DiscreteVector<DDims...> const &level,
+                 ddc::DiscreteVector<DDims...> const &maximum_level) {
+  check_levels(level, maximum_level);
+  auto const l = levels_of(level);
+  auto const L = levels_of(maximum_level);
   std::array<long, sizeof...(DDims)> la{}, La{};
   for (size_t i = 0; i < l.size(); ++i) {
     la[i] = static_cast<long>(l[i]);
     La[i] = static_cast<long>(L[i]);
   }
-  if (!(grid.domain() == strided_domain_from_level<DDims...>(la, La)))
-    throw std::invalid_argument(
-        "the GPU transform needs the complete grid of the level");
+  return grid.domain() == strided_domain_from_level<DDims...>(la, La);
 }
+
+// The box of the level lattice that a partial chunk holds: front uids and
+// extents per dimension. Its strides must be the level's spacing.
+template <class ChunkSpanType, class... DDims>
+void window_of(ChunkSpanType const &grid,
+               ddc::DiscreteVector<DDims...> const &level,
+               ddc::DiscreteVector<DDims...> const &maximum_level,
+               std::array<int64_t, sizeof...(DDims)> &front,
+               std::array<int64_t, sizeof...(DDims)> &extents) {
+  auto const l = levels_of(level);
+  auto const L = levels_of(maximum_level);
+  auto const dom = grid.domain();
+  size_t i = 0;
+  ((front[i] = static_cast<int64_t>(dom.front().template uid<DDims>()),
+    extents[i] = static_cast<int64_t>(dom.extents().template get<DDims>()),
+    static_cast<int64_t>(dom.strides().template get<DDims>()) ==
+            (int64_t{1} << (L[i] - l[i]))
+        ? void(++i)
+        : throw std::invalid_argument(
+              "the chunk's strides must be the level's spacing")),
+   ...);
+}
+
+// transform_in along dimension `dim` of a partial chunk (C ABI
+// paliwa_gb_transform_in_window).
+template <class ChunkSpanType, class... DDims>
+void transform_window(ChunkSpanType const &grid,
+                      ddc::DiscreteVector<DDims...> const &level,
+                      ddc::DiscreteVector<DDims...> const &maximum_level,
+                      int dim, std::vector<int64_t> const &levels,
+                      LiftingPasses const &filters, void *stream) {
+  using T = typename ChunkSpanType::element_type;
+  constexpr size_t n = sizeof...(DDims);
+  std::array<int64_t, n> front{}, extents{};
+  window_of(grid, level, maximum_level, front, extents);
+  auto const lv = levels_of(level);
+  auto const lm = levels_of(maximum_level);
+  std::vector<int32_t> offs;
+  std::vector<double> co;
+  for (auto const &[o, f] : filters) {
+    offs.push_back(o);
+    co.insert(co.end(), f.begin(), f.end());
+  }
+  check(paliwa_gb_transform_in_window(
+      static_cast<void *>(grid.data_handle()), dtype_of<T>(),
+      static_cast<int>(n), lv.data(), lm.data(), front.data(), extents.data(),
+      dim, levels.data(), static_cast<int>(levels.size()), offs.data(),
+      co.data(), static_cast<int>(offs.size()), stream));
+}
+
+// Levels level[dim] .. lmin+1 (forward) or lmin+1 .. level[dim] (inverse)
+// of hierarchize_in / dehierarchize_in (paliwa_transform.hpp:346-399).
+template <class... DDims>
+std::vector<int64_t> level_range(ddc::DiscreteVector<DDims...> const &level,
+                                 ddc::DiscreteVector<DDims...> const &minimum,
+                                 ddc::DiscreteVector<DDims...> const &maximum,
+                                 int dim, bool forward) {
+  auto const l = levels_of(level)[dim];
+  auto const m = levels_of(minimum)[dim];
+  if (m < 0 || m > l || l > levels_of(maximum)[dim])
+    throw std::invalid_argument(
+        "requires 0 <= minimum_level <= level <= maximum_level");
+  std::vector<int64_t> r;
+  for (int64_t k = m + 1; k <= l; ++k) r.push_back(k);
+  if (forward) std::reverse(r.begin(), r.end());
+  return r;
+}
+
 } // namespace gb300
 
+// transform_in<Dim> (full-grid overload, paliwa_transform.hpp:215-251):
+// every level of `levels` in order, the filters of each in order. A chunk
+// holding the complete lattice runs the GPU's tiled transform; any other
+// chunk (a box of the lattice) the bounds-checked passes of the reference.
 template <class Dim, class ChunkSpanType, class LevelRange,
           class ExecSpace = gb300::Stream, class... Dims>
 constexpr bool
@@ -154,12 +222,17 @@ transform_in(ChunkSpanType grid, ddc::DiscreteVector<Dims...> const &level,
              ddc::DiscreteVector<Dims...> const &maximum_level,
              LevelRange const &levels, LiftingPasses const &filters,
              ExecSpace instance = ExecSpace()) {
-  gb300::check_complete(grid, level, maximum_level);
   using T = typename ChunkSpanType::element_type;
-  auto const lv = gb300::levels_of(level);
-  auto const lm = gb300::levels_of(maximum_level);
   std::vector<int64_t> ls;
   for (auto l : levels) ls.push_back(static_cast<int64_t>(l));
+  if (!gb300::is_complete(grid, level, maximum_level)) {
+    gb300::transform_window(grid, level, maximum_level,
+                            gb300::dim_index<Dim, Dims...>(), ls, filters,
+                            gb300::stream_of(instance));
+    return true;
+  }
+  auto const lv = gb300::levels_of(level);
+  auto const lm = gb300::levels_of(maximum_level);
   std::vector<int32_t> offs;
   std::vector<double> co;
   for (auto const &[o, f] : filters) {
@@ -175,6 +248,39 @@ transform_in(ChunkSpanType grid, ddc::DiscreteVector<Dims...> const &level,
   return true;
 }
 
+namespace gb300 {
+template <class Dim, bool Forward, class ChunkSpanType, class ExecSpace,
+          class... DDims>
+bool transform_axis(ChunkSpanType const grid,
+                    ddc::DiscreteVector<DDims...> const &level,
+                    ddc::DiscreteVector<DDims...> const &minimum_level,
+                    ddc::DiscreteVector<DDims...> const &maximum_level,
+                    std::string const &wavelet_name, ExecSpace instance) {
+  using T = typename ChunkSpanType::element_type;
+  int const dim = dim_index<Dim, DDims...>();
+  if (!is_complete(grid, level, maximum_level)) {
+    auto const &filters =
+        (Forward ? lifting_wavelet_filter_offsets_and_coefficients
+                 : lifting_wavelet_reconstruct_offsets_and_coefficients)
+            .at(wavelet_name);
+    auto const ls = level_range(level, minimum_level, maximum_level, dim,
+                                Forward);
+    transform_window(grid, level, maximum_level, dim, ls, filters,
+                     stream_of(instance));
+    return true;
+  }
+  auto const lv = levels_of(level);
+  auto const ln = levels_of(minimum_level);
+  auto const lm = levels_of(maximum_level);
+  check((Forward ? paliwa_gb_hierarchize_in : paliwa_gb_dehierarchize_in)(
+      static_cast<void *>(grid.data_handle()), dtype_of<T>(),
+      static_cast<int>(lv.size()), lv.data(), ln.data(), lm.data(), dim,
+      wavelet_id(wavelet_name), stream_of(instance)));
+  return true;
+}
+} // namespace gb300
+
+// hierarchize_in<Dim> / dehierarchize_in<Dim> (paliwa_transform.hpp:346-399).
 template <class DDimInWhichToHierarchize, class ChunkSpanType,
           class ExecSpace = gb300::Stream, class... DDims>
 constexpr bool
@@ -184,17 +290,9 @@ hierarchize_in(ChunkSpanType const strided_grid,
                ddc::DiscreteVector<DDims...> const &maximum_level,
                std::string const &wavelet_name = "hat",
                ExecSpace instance = ExecSpace()) {
-  gb300::check_complete(strided_grid, level, maximum_level);
-  using T = typename ChunkSpanType::element_type;
-  auto const lv = gb300::levels_of(level);
-  auto const ln = gb300::levels_of(minimum_level);
-  auto const lm = gb300::levels_of(maximum_level);
-  gb300::check(paliwa_gb_hierarchize_in(
-      static_cast<void *>(strided_grid.data_handle()), gb300::dtype_of<T>(),
-      static_cast<int>(lv.size()), lv.data(), ln.data(), lm.data(),
-      gb300::dim_index<DDimInWhichToHierarchize, DDims...>(),
-      gb300::wavelet_id(wavelet_name), gb300::stream_of(instance)));
-  return true;
+  return gb300::transform_axis<DDimInWhichToHierarchize, true>(
+      strided_grid, level, minimum_level, maximum_level, wavelet_name,
+      instance);
 }
 
 template <class DDimInWhichToHierarchize, class ChunkSpanType,
@@ -206,19 +304,13 @@ dehierarchize_in(ChunkSpanType const strided_grid,
                  ddc::DiscreteVector<DDims...> const &maximum_level,
                  std::string const &wavelet_name = "hat",
                  ExecSpace instance = ExecSpace()) {
-  gb300::check_complete(strided_grid, level, maximum_level);
-  using T = typename ChunkSpanType::element_type;
-  auto const lv = gb300::levels_of(level);
-  auto const ln = gb300::levels_of(minimum_level);
-  auto const lm = gb300::levels_of(maximum_level);
-  gb300::check(paliwa_gb_dehierarchize_in(
-      static_cast<void *>(strided_grid.data_handle()), gb300::dtype_of<T>(),
-      static_cast<int>(lv.size()), lv.data(), ln.data(), lm.data(),
-      gb300::dim_index<DDimInWhichToHierarchize, DDims...>(),
-      gb300::wavelet_id(wavelet_name), gb300::stream_of(instance)));
-  return true;
+  return gb300::transform_axis<DDimInWhichToHierarchize, false>(
+      strided_grid, level, minimum_level, maximum_level, wavelet_name,
+      instance);
 }
 
+// hierarchize / dehierarchize (paliwa_transform.hpp:401-431): every
+// dimension in declaration order.
 template <class ChunkSpanType, class ExecSpace = gb300::Stream,
           class... DDims>
 constexpr void hierarchize(ChunkSpanType const strided_grid,
@@ -227,8 +319,13 @@ constexpr void hierarchize(ChunkSpanType const strided_grid,
                            ddc::DiscreteVector<DDims...> const &maximum_level,
                            std::string const &wavelet_name = "hat",
                            ExecSpace instance = ExecSpace()) {
-  gb300::check_complete(strided_grid, level, maximum_level);
   using T = typename ChunkSpanType::element_type;
+  if (!gb300::is_complete(strided_grid, level, maximum_level)) {
+    (hierarchize_in<DDims>(strided_grid, level, minimum_level, maximum_level,
+                           wavelet_name, instance),
+     ...);
+    return;
+  }
   auto const lv = gb300::levels_of(level);
   auto const ln = gb300::levels_of(minimum_level);
   auto const lm = gb300::levels_of(maximum_level);
@@ -246,8 +343,13 @@ constexpr void dehierarchize(ChunkSpanType const strided_grid,
                              ddc::DiscreteVector<DDims...> const &maximum_level,
                              std::string const &wavelet_name = "hat",
                              ExecSpace instance = ExecSpace()) {
-  gb300::check_complete(strided_grid, level, maximum_level);
   using T = typename ChunkSpanType::element_type;
+  if (!gb300::is_complete(strided_grid, level, maximum_level)) {
+    (dehierarchize_in<DDims>(strided_grid, level, minimum_level,
+                             maximum_level, wavelet_name, instance),
+     ...);
+    return;
+  }
   auto const lv = gb300::levels_of(level);
   auto const ln = gb300::levels_of(minimum_level);
   auto const lm = gb300::levels_of(maximum_level);
@@ -255,56 +357,6 @@ constexpr void dehierarchize(ChunkSpanType const strided_grid,
       static_cast<void *>(strided_grid.data_handle()), gb300::dtype_of<T>(),
       static_cast<int>(lv.size()), lv.data(), ln.data(), lm.data(),
       gb300::wavelet_id(wavelet_name), gb300::stream_of(instance)));
-}
-
-// paliwa_domains.hpp:454-469: visit every uid of per-level bounds (level 0:
-// multiples of the period; level h: odd points of level h).
-template <typename Dim, typename Visit>
-void for_each_transform_index(std::vector<PeriodicBounds> const &bounds,
-                              long maximum_level, Visit visit) {
-  long const period = 1L << maximum_level;
-  for (size_t h = 0; h < bounds.size(); ++h) {
-    auto const b = bounds[h];
-    if (b.empty()) continue;
-    long const stride = h == 0 ? period : 2L << (maximum_level - h);
-    long const last = b.max + (b.min > b.max ? period : 0);
-    for (long x = b.min; x <= last; x += stride)
-      visit(ddc::DiscreteElement<Dim>(x % period));
-  }
-}
-
-// paliwa_domains.hpp:540-567: the points of `domain` whose uid along Dim
-// lies in the periodic bounds, as at most two strided domains (a wrapped
-// interval splits at the period); the lattice of `domain` is kept.
-template <typename Dim, typename... Dims>
-std::vector<ddc::StridedDiscreteDomain<Dims...>>
-restrict_periodic_bounds(ddc::StridedDiscreteDomain<Dims...> const &domain,
-                         PeriodicBounds bounds, long period) {
-  std::vector<ddc::StridedDiscreteDomain<Dims...>> parts;
-  if (bounds.empty() || domain.size() == 0) return parts;
-  long const first = static_cast<long>(domain.front().template uid<Dim>());
-  long const stride = static_cast<long>(domain.strides().template get<Dim>());
-  long const last =
-      first + (static_cast<long>(domain.extents().template get<Dim>()) - 1) *
-                  stride;
-  auto add = [&](long lo, long hi) {
-    lo = std::max(lo, first);
-    hi = std::min(hi, last);
-    long const begin = first + ((lo - first + stride - 1) / stride) * stride;
-    if (begin > hi) return;
-    auto f = domain.front();
-    f.template uid<Dim>() = begin;
-    auto e = domain.extents();
-    e.template get<Dim>() = (hi - begin) / stride + 1;
-    parts.emplace_back(f, e, domain.strides());
-  };
-  if (bounds.min <= bounds.max) {
-    add(bounds.min, bounds.max);
-  } else {
-    add(bounds.min, period - 1);
-    add(0, bounds.max);
-  }
-  return parts;
 }
 
 // Restricted-output transform (paliwa_transform.hpp:333-344): the lifting

@@ -66,6 +66,10 @@ const char *paliwa_gb_last_error(void);
 /* Library ABI version (major * 10000 + minor * 100 + patch). */
 int paliwa_gb_version(void);
 
+/* Waits for the work queued on `stream` (the fence() of an execution-space
+ * instance, paliwa/paliwa_utils.hpp:27-32). */
+int paliwa_gb_synchronize(void *stream);
+
 /* Wavelet name -> id. Unknown names return PALIWA_GB_OUT_OF_RANGE, as
  * lifting_wavelet_filter_offsets_and_coefficients.at(name) throws
  * std::out_of_range (paliwa/paliwa_transform.hpp:370, 397). */

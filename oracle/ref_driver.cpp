@@ -407,4 +407,49 @@ int ref_hierarchical_subspaces(int ndim, long const *nodal_level, int capacity,
   });
 }
 
+// paliwa::restrict_periodic_bounds<DDimA> (paliwa_domains.hpp:539-568) of a
+// 2D strided domain: up to 2 parts of 6 values (front, extents, strides).
+int ref_restrict_periodic_bounds(long const *front, long const *extents,
+                                 long const *strides, long bmin, long bmax,
+                                 long period, int *nparts, long *out) {
+  return guarded([&] {
+    using namespace paliwa;
+    ddc::StridedDiscreteDomain<DDimA, DDimB> const d{
+        ddc::DiscreteElement<DDimA, DDimB>(front[0], front[1]),
+        ddc::DiscreteVector<DDimA, DDimB>(extents[0], extents[1]),
+        ddc::DiscreteVector<DDimA, DDimB>(strides[0], strides[1])};
+    auto const parts = paliwa::restrict_periodic_bounds<DDimA>(
+        d, paliwa::PeriodicBounds{bmin, bmax}, period);
+    *nparts = static_cast<int>(parts.size());
+    for (std::size_t i = 0; i < parts.size() && i < 2; ++i) {
+      auto const &p = parts[i];
+      long *o = out + 6 * i;
+      o[0] = static_cast<long>(p.front().template uid<DDimA>());
+      o[1] = static_cast<long>(p.front().template uid<DDimB>());
+      o[2] = p.extents().template get<DDimA>();
+      o[3] = p.extents().template get<DDimB>();
+      o[4] = p.strides().template get<DDimA>();
+      o[5] = p.strides().template get<DDimB>();
+    }
+  });
+}
+
+// paliwa::for_each_transform_index (paliwa_domains.hpp:437-450): the visited
+// uids of per-level bounds (2 * nb values).
+int ref_for_each_transform_index(long const *bounds, int nb,
+                                 long maximum_level, int capacity, long *count,
+                                 long *out) {
+  return guarded([&] {
+    std::vector<paliwa::PeriodicBounds> b(nb);
+    for (int i = 0; i < nb; ++i) b[i] = {bounds[2 * i], bounds[2 * i + 1]};
+    long n = 0;
+    paliwa::for_each_transform_index<paliwa::DDimA>(
+        b, maximum_level, [&](ddc::DiscreteElement<paliwa::DDimA> e) {
+          if (n < capacity) out[n] = static_cast<long>(e.uid());
+          ++n;
+        });
+    *count = n;
+  });
+}
+
 } // extern "C"

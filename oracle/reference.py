@@ -205,3 +205,27 @@ def hierarchical_subspaces(nodal_level):
     _check(lib().ref_hierarchical_subspaces(d, _longs(nodal_level), cap,
                                             ctypes.byref(cnt), out))
     return [tuple(out[i * d:(i + 1) * d]) for i in range(cnt.value)]
+
+
+def restrict_periodic_bounds_2d(front, extents, strides, bounds, period):
+    """paliwa::restrict_periodic_bounds along dimension 0 of a 2D strided
+    domain: a list of (front, extents, strides) parts."""
+    n = ctypes.c_int()
+    out = (ctypes.c_long * 12)()
+    _check(lib().ref_restrict_periodic_bounds(
+        _longs(front), _longs(extents), _longs(strides),
+        ctypes.c_long(bounds[0]), ctypes.c_long(bounds[1]),
+        ctypes.c_long(period), ctypes.byref(n), out))
+    return [(tuple(out[6 * i:6 * i + 2]), tuple(out[6 * i + 2:6 * i + 4]),
+             tuple(out[6 * i + 4:6 * i + 6])) for i in range(n.value)]
+
+
+def for_each_transform_index(bounds, maximum_level):
+    flat = [v for b in bounds for v in b]
+    cap = 1 << 16
+    out = (ctypes.c_long * cap)()
+    n = ctypes.c_long()
+    _check(lib().ref_for_each_transform_index(
+        _longs(flat), len(bounds), ctypes.c_long(maximum_level), cap,
+        ctypes.byref(n), out))
+    return list(out[:n.value])

@@ -35,6 +35,7 @@ _pd = ctypes.POINTER(ctypes.c_double)
 SIGNATURES = {
     "paliwa_gb_last_error": (ctypes.c_char_p, []),
     "paliwa_gb_version": (_i, []),
+    "paliwa_gb_synchronize": (_i, [_vp]),
     "paliwa_gb_wavelet_id": (_i, [ctypes.c_char_p, ctypes.POINTER(_i)]),
     "paliwa_gb_wavelet_filters": (_i, [_i, _i, ctypes.POINTER(_i), _pi32, _pd]),
     "paliwa_gb_transform_in": (

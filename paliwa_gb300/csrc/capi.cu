@@ -567,6 +567,13 @@ const char *paliwa_gb_last_error(void) { return g_last_error.c_str(); }
 
 int paliwa_gb_version(void) { return 100; }
 
+int paliwa_gb_synchronize(void *stream) {
+  return guarded([&] {
+    cuda_check(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)),
+               "cudaStreamSynchronize");
+  });
+}
+
 int paliwa_gb_wavelet_id(const char *name, int *id) {
   return guarded([&] {
     if (name == nullptr || id == nullptr)

@@ -12,8 +12,12 @@
 #include <stdexcept>
 #include <vector>
 
+#include <paliwa/paliwa_dimensions.hpp>
+#include <paliwa/paliwa_domains.hpp>
 #include <paliwa/paliwa_io.hpp>
 #include <paliwa/paliwa_transform.hpp>
+#include <paliwa/paliwa_utils.hpp>
+#include <paliwa/paliwa_wavelets.hpp>
 
 #include "paliwa_oracle.hpp"
 
@@ -57,10 +61,11 @@ int main() {
   EXPECT(throws<std::invalid_argument>([&] {
     paliwa::hierarchize(fake, level, Vec(6, 0, 0), lmax, "hat");
   }));
-  Dom const part(dom.front(), Vec(16, 8, 16), dom.strides());
-  ddc::ChunkSpan<double, Dom> partial(reinterpret_cast<double *>(256), part);
+  // A chunk that is not a box of the level's lattice (wrong strides).
+  Dom const skew(dom.front(), Vec(16, 8, 16), Vec(1, 1, 1));
+  ddc::ChunkSpan<double, Dom> skewed(reinterpret_cast<double *>(256), skew);
   EXPECT(throws<std::invalid_argument>(
-      [&] { paliwa::hierarchize(partial, level, lmin, lmax, "hat"); }));
+      [&] { paliwa::hierarchize(skewed, level, lmin, lmax, "hat"); }));
 
   // Restricted-output planning (paliwa_domains.hpp), host only: the
   // reference's known answers (test/test_paliwa_plan.cpp:199-221, 403-429).
@@ -248,6 +253,39 @@ int main() {
     EXPECT(cudaMemcpy(part.data(), dev, part.size() * sizeof(double),
                       cudaMemcpyDeviceToHost) == cudaSuccess);
     EXPECT(part == full);
+  }
+  // A chunk holding a box of the lattice (a partial chunk): the reference's
+  // bounds-checked passes, dimension by dimension, against the oracle.
+  {
+    Dom const box(Dom::discrete_element_type(std::array<long, 3>{8, 2, 6}),
+                  Vec(9, 5, 7), dom.strides());
+    std::vector<double> bhost(box.size());
+    for (auto &v : bhost) v = u(rng);
+    double *bdev = nullptr;
+    EXPECT(cudaMalloc(&bdev, bhost.size() * sizeof(double)) == cudaSuccess);
+    EXPECT(cudaMemcpy(bdev, bhost.data(), bhost.size() * sizeof(double),
+                      cudaMemcpyHostToDevice) == cudaSuccess);
+    ddc::ChunkSpan<double, Dom> part(bdev, box);
+    paliwa::hierarchize(part, level, lmin, lmax, "biorthogonal", instance);
+    instance.fence();
+    std::vector<double> got(bhost.size()), want = bhost;
+    EXPECT(cudaMemcpy(got.data(), bdev, got.size() * sizeof(double),
+                      cudaMemcpyDeviceToHost) == cudaSuccess);
+    paliwa_oracle::Shape shape;
+    shape.ndim = 3;
+    shape.level = {5, 3, 4};
+    shape.maximum_level = {6, 3, 5};
+    long const front[3] = {8, 2, 6}, ext[3] = {9, 5, 7};
+    long const low[3] = {1, 0, 2}, high[3] = {5, 3, 4};
+    auto const f = paliwa_oracle::forward_filters(1);
+    for (int d = 0; d < 3; ++d) {
+      std::vector<long> ls;
+      for (long k = high[d]; k > low[d]; --k) ls.push_back(k);
+      paliwa_oracle::transform_in_window(want.data(), shape, front, ext, d, ls,
+                                         f);
+    }
+    EXPECT(got == want);
+    cudaFree(bdev);
   }
   // Raw dump (paliwa_io.hpp): storage order, no header.
   {

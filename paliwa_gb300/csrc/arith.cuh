@@ -32,11 +32,9 @@ template <typename T, bool ExactProducts> struct Plain {
   static __device__ __forceinline__ V load(Store x) { return x; }
   static __device__ __forceinline__ Store store(V x) { return x; }
 
-  static constexpr bool kHasFp64Mode = false;
   static constexpr bool kPacked = false;
 
   // C1: the middle coefficient is exactly 1 (skips one multiply).
-  // F64: unused (plain arithmetic has a single precision).
   static __device__ __forceinline__ T k0(Coeffs const &c) {
     if constexpr (sizeof(T) == 8) return c.c0; else return c.f0;
   }
@@ -47,7 +45,7 @@ template <typename T, bool ExactProducts> struct Plain {
     if constexpr (sizeof(T) == 8) return c.c2; else return c.f2;
   }
 
-  template <bool C1, bool F64>
+  template <bool C1>
   static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
                                              V up) {
     if constexpr (ExactProducts) {
@@ -88,10 +86,11 @@ template <typename T, bool ExactProducts> struct Plain {
 // with l = 0. Each update evaluates c0*lo + c1*me + c2*up with error-free
 // transformations (FMA-based TwoProd, Knuth TwoSum), so rounding errors do not
 // accumulate along the level chain; the pair is rounded to one float only
-// when it is stored, i.e. once per dimension. An FP64 mode for the coarsest
-// levels exists (LiftParams::fp64_log2_points) but is off by default: on
-// GB300 those per-pencil steps occupy the FP64 pipe for whole warp
-// instructions with one to four active lanes.
+// when it is stored, i.e. once per dimension. Every level runs in this
+// arithmetic, the coarsest included: its 48-bit significand is far below
+// the float storage that every value is rounded to, so FP64 steps would not
+// change what is stored (the mass-conservation tests hold the FP32c result
+// to the storage-rounding bound).
 struct DF {
   float h, l;
 };
@@ -132,26 +131,13 @@ template <bool Sym> struct CompensatedT {
   static __device__ __forceinline__ Store store(V x) {
     return __fadd_rn(x.h, x.l);
   }
-  static constexpr bool kHasFp64Mode = true;
   // Wavelet schedules may run the fine levels on packed pairs (sym_update2).
   static constexpr bool kPacked = Sym;
 
-  static __device__ __forceinline__ double to_double(DF x) {
-    return double(x.h) + double(x.l);
-  }
-  static __device__ __forceinline__ DF from_double(double d) {
-    float h = __double2float_rn(d);
-    return {h, __double2float_rn(d - double(h))};
-  }
-  template <bool C1, bool F64>
+  template <bool C1>
   static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
                                              V up) {
-    if constexpr (F64) {
-      double const m = to_double(me);
-      double t = C1 ? m : __dmul_rn(c.c1, m);
-      t = __fma_rn(c.c0, to_double(lo), t);
-      return from_double(__fma_rn(c.c2, to_double(up), t));
-    } else if constexpr (Sym) {
+    if constexpr (Sym) {
       float const cc = c.f0;
       DF const s = two_sum(lo.h, up.h);
       float const e1 = __fadd_rn(s.l, __fadd_rn(lo.l, up.l));
@@ -278,7 +264,6 @@ struct RowF32 {
   using Store = uint4;
   using Elem = float;
   static constexpr int kCols = 4;
-  static constexpr bool kHasFp64Mode = false;
   static constexpr bool kPacked = false;
   static __device__ __forceinline__ V load(Store u) {
     return {f2_bits(u.x, u.y), f2_bits(u.z, u.w)};
@@ -294,7 +279,7 @@ struct RowF32 {
     t = f2_fma(f2_splat(c.f0), lo, t);
     return f2_fma(f2_splat(c.f2), up, t);
   }
-  template <bool C1, bool F64>
+  template <bool C1>
   static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
                                              V up) {
     return {pair<C1>(c, lo.a, me.a, up.a), pair<C1>(c, lo.b, me.b, up.b)};
@@ -307,7 +292,6 @@ struct RowF32C {
   using Store = uint2;
   using Elem = float;
   static constexpr int kCols = 2;
-  static constexpr bool kHasFp64Mode = false;
   static constexpr bool kPacked = false;
   static __device__ __forceinline__ V load(Store u) {
     return {f2_bits(u.x, u.y), 0ull};
@@ -316,7 +300,7 @@ struct RowF32C {
     f2 const s = f2_add(v.h, v.l);
     return {f2_lo(s), f2_hi(s)};
   }
-  template <bool C1, bool F64>
+  template <bool C1>
   static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
                                              V up) {
     return sym_update2<C1>(c, lo, me, up);
@@ -332,16 +316,15 @@ struct RowF64 {
   using Store = double2;
   using Elem = double;
   static constexpr int kCols = 2;
-  static constexpr bool kHasFp64Mode = false;
   static constexpr bool kPacked = false;
   static __device__ __forceinline__ V load(Store u) { return {u.x, u.y}; }
   static __device__ __forceinline__ Store store(V v) { return {v.x, v.y}; }
-  template <bool C1, bool F64>
+  template <bool C1>
   static __device__ __forceinline__ V update(Coeffs const &c, V lo, V me,
                                              V up) {
     using P = Plain<double, true>;
-    return {P::template update<C1, F64>(c, lo.x, me.x, up.x),
-            P::template update<C1, F64>(c, lo.y, me.y, up.y)};
+    return {P::template update<C1>(c, lo.x, me.x, up.x),
+            P::template update<C1>(c, lo.y, me.y, up.y)};
   }
 };
 

@@ -144,7 +144,6 @@ LiftParams launch_params(std::vector<Filter> const &filters) {
   // pipe even when only one lane is active; measured, they cost more than
   // the rest of the FP32-compensated transform. The coarsest levels
   // therefore stay in double-float arithmetic unless enabled here.
-  p.fp64_log2_points = -1;
   for (size_t i = 0; i < filters.size(); ++i) {
     if (filters[i].offset != 0 && filters[i].offset != 1)
       throw StatusError(PALIWA_GB_RUNTIME_ERROR, "Filter offset not supported");
@@ -452,7 +451,6 @@ void launch_lift(int dtype, bool exact, bool symmetric, int sched, int R,
   params.njobs = njobs;
   params.total_tiles = total_tiles;
   params.rounds = kRounds;
-  if (params.fp64_log2_points >= 0) sched = -1;
   if (R == kCopy) return launch_copy(params, s);
   if (R > kWide) {  // the wide and tile kernels
     switch (dtype) {

@@ -65,7 +65,6 @@ struct LiftParams {
   int njobs;
   long long total_tiles;
   int npasses;
-  int fp64_log2_points; // steps updating <= 2^this points per pencil in FP64
   int rounds;           // column rounds per tile (tile = rounds * NT * R)
   unsigned c1_one_mask;
   int offsets[kMaxPasses];
@@ -96,63 +95,51 @@ __device__ __forceinline__ V tail_value(V const (&v)[R], int sh) {
 // One fine step (distance S < R) on the chunk held in registers. `nb` is the
 // neighbour from the adjacent chunk: for odd passes (offset 1) the next
 // chunk's slot 0, for even passes (offset 0) the previous chunk's slot R - S.
-template <class A, int R, int S, bool C1, bool F64, typename V>
+template <class A, int R, int S, bool C1, typename V>
 __device__ __forceinline__ void fine_step(V (&v)[R], int o, V nb,
                                           Coeffs const &cf) {
   if (o == 1) {
 #pragma unroll
     for (int j = S; j < R; j += 2 * S) {
       V up = (j + S < R) ? v[(j + S) % R] : nb;
-      v[j] = A::template update<C1, F64>(cf, v[j - S], v[j], up);
+      v[j] = A::template update<C1>(cf, v[j - S], v[j], up);
     }
   } else {
 #pragma unroll
     for (int j = 0; j < R; j += 2 * S) {
       V lo = (j >= S) ? v[(j + R - S) % R] : nb;
-      v[j] = A::template update<C1, F64>(cf, lo, v[j], v[j + S]);
+      v[j] = A::template update<C1>(cf, lo, v[j], v[j + S]);
     }
   }
 }
 
 // Selects the compile-time distance 2^K == 2^sh (sh < log2 R).
-template <class A, int R, bool C1, bool F64, int K = 0, typename V>
+template <class A, int R, bool C1, int K = 0, typename V>
 __device__ __forceinline__ void fine_distance(V (&v)[R], int sh, int o, V nb,
                                               Coeffs const &cf) {
   if constexpr ((1 << K) < R) {
     if (sh == K) {
-      fine_step<A, R, (1 << K), C1, F64>(v, o, nb, cf);
+      fine_step<A, R, (1 << K), C1>(v, o, nb, cf);
       return;
     }
-    fine_distance<A, R, C1, F64, K + 1>(v, sh, o, nb, cf);
+    fine_distance<A, R, C1, K + 1>(v, sh, o, nb, cf);
   }
 }
 
 template <class A, int R, typename V>
 __device__ __forceinline__ void fine_dispatch(V (&v)[R], int sh, int o, V nb,
-                                              Coeffs const &cf, bool c1one,
-                                              bool f64) {
-  if (A::kHasFp64Mode && f64) {
-    if (c1one)
-      fine_distance<A, R, true, A::kHasFp64Mode>(v, sh, o, nb, cf);
-    else
-      fine_distance<A, R, false, A::kHasFp64Mode>(v, sh, o, nb, cf);
-  } else {
-    if (c1one)
-      fine_distance<A, R, true, false>(v, sh, o, nb, cf);
-    else
-      fine_distance<A, R, false, false>(v, sh, o, nb, cf);
-  }
+                                              Coeffs const &cf, bool c1one) {
+  if (c1one)
+    fine_distance<A, R, true>(v, sh, o, nb, cf);
+  else
+    fine_distance<A, R, false>(v, sh, o, nb, cf);
 }
 
 template <class A, typename V>
-__device__ __forceinline__ V coarse_update(Coeffs const &cf, bool c1one,
-                                           bool f64, V lo, V me, V up) {
-  if (A::kHasFp64Mode && f64) {
-    if (c1one) return A::template update<true, A::kHasFp64Mode>(cf, lo, me, up);
-    return A::template update<false, A::kHasFp64Mode>(cf, lo, me, up);
-  }
-  if (c1one) return A::template update<true, false>(cf, lo, me, up);
-  return A::template update<false, false>(cf, lo, me, up);
+__device__ __forceinline__ V coarse_update(Coeffs const &cf, bool c1one, V lo,
+                                           V me, V up) {
+  if (c1one) return A::template update<true>(cf, lo, me, up);
+  return A::template update<false>(cf, lo, me, up);
 }
 
 // Warp shuffles of one value (double, float or a double-float pair).
@@ -302,7 +289,6 @@ struct RuntimeSched {
     int const nlev = job.nlevels;
     for (int li = 0; li < nlev; ++li) {
       int const sh = job.shift[li];
-      bool const f64 = (job.log2_n - sh - 1) <= p.fp64_log2_points;
       for (int ps = 0; ps < p.npasses; ++ps) {
         int const o = p.offsets[ps];
         Coeffs const cf = p.coeffs[ps];
@@ -310,11 +296,11 @@ struct RuntimeSched {
         if (sh < LOG2R) {
           V const pub = (o == 1) ? v[0] : tail_value<R>(v, sh);
           V const nb = ctx.fine_neighbor(o, pub);
-          fine_dispatch<A, R>(v, sh, o, nb, cf, c1one, f64);
+          fine_dispatch<A, R>(v, sh, o, nb, cf, c1one);
           ctx.fine_wrote_heads(o);
         } else {
           ctx.coarse(v[0], o, 1 << (sh - LOG2R), [&](V lo, V me, V up) {
-            return coarse_update<A>(cf, c1one, f64, lo, me, up);
+            return coarse_update<A>(cf, c1one, lo, me, up);
           });
         }
       }
@@ -378,13 +364,13 @@ template <int W, bool FWD> struct WaveletSched {
 #pragma unroll
       for (int j = S; j < R; j += 2 * S) {
         V const up = (j + S < R) ? v[(j + S) % R] : nb;
-        v[j] = A::template update<P::c1one, false>(cf, v[j - S], v[j], up);
+        v[j] = A::template update<P::c1one>(cf, v[j - S], v[j], up);
       }
     } else {
 #pragma unroll
       for (int j = 0; j < R; j += 2 * S) {
         V const lo = (j >= S) ? v[(j + R - S) % R] : nb;
-        v[j] = A::template update<P::c1one, false>(cf, lo, v[j], v[j + S]);
+        v[j] = A::template update<P::c1one>(cf, lo, v[j], v[j + S]);
       }
     }
     ctx.fine_wrote_heads(P::offset);
@@ -405,7 +391,7 @@ template <int W, bool FWD> struct WaveletSched {
     (ctx.coarse(v[0], P::offset, d,
                 [](V lo, V me, V up) {
                   constexpr Coeffs cf = P::coeffs();
-                  return A::template update<P::c1one, false>(cf, lo, me, up);
+                  return A::template update<P::c1one>(cf, lo, me, up);
                 }),
      ...);
   }
@@ -473,10 +459,10 @@ template <int W, bool FWD> struct WaveletSched {
       V sH = {f2_y(q[0].h), f2_y(q[0].l)};  // slot H
       if constexpr (P::offset == 1) {
         V const nb = ctx.fine_neighbor(1, s0);
-        sH = A::template update<P::c1one, false>(cf, s0, sH, nb);
+        sH = A::template update<P::c1one>(cf, s0, sH, nb);
       } else {
         V const nb = ctx.fine_neighbor(0, sH);  // previous chunk's slot H
-        s0 = A::template update<P::c1one, false>(cf, nb, s0, sH);
+        s0 = A::template update<P::c1one>(cf, nb, s0, sH);
         ctx.fine_wrote_heads(0);
       }
       q[0].h = f2_pack(s0.h, sH.h);

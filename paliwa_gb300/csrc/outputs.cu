@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kOutThreads) out_pass_kernel(OutPass const p) 
     T const vm = g[off + ix * es];
     T const vu = g[off + iu * es];
     g[off + ix * es] =
-        A::template update<false, false>(p.c, vl, vm, vu);
+        A::template update<false>(p.c, vl, vm, vu);
   }
 }
 

@@ -247,6 +247,18 @@ int paliwa_gb_batch_use_graphs(paliwa_gb_batch *batch, int enable);
  * reference (its CT driver spreads grids over execution-space instances,
  * test/test_paliwa_combination_technique.cpp:164-174). */
 int paliwa_gb_batch_set_groups(paliwa_gb_batch *batch, int ngroups);
+/* enable != 0 (default): grids whose trailing axes span blocks ("slabs") of
+ * at most 32 KB, with levels to transform along two or more of those axes,
+ * transform all of them in one launch of the slab kernel (one HBM pass over
+ * the grid, tiles moved by the tensor memory accelerator); 0 plans every
+ * axis on its own. Results are the same bits either way. Re-plans both
+ * directions after synchronizing the device. No counterpart in the
+ * reference. */
+int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable);
+/* PALIWA_GB_TIMEOUT if a slab launch of this batch gave up a bounded wait
+ * for its tile copies since the last call (the flag is then cleared);
+ * otherwise PALIWA_GB_OK. Synchronizes with the device. */
+int paliwa_gb_batch_status(paliwa_gb_batch *batch);
 int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
                          int64_t *launches_forward,
                          int64_t *launches_inverse);
@@ -259,7 +271,9 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
  * the last axis, 192 + R and 256 + R the tile kernel (row-major tiles in
  * shared memory, rows of adjacent columns in registers) for pencils of up to
  * 32 chunks and longer ones, 512 the flat copy of windowed stages' results
- * back into the grids; `kernels` may be null. Call with
+ * back into the grids, 1024 the slab kernel (every level of a grid's
+ * trailing axes in one pass; its bytes count one read and one write of each
+ * point); `kernels` may be null. Call with
  * capacity 0 to get *nlaunches first. */
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,

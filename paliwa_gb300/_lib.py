@@ -59,6 +59,8 @@ SIGNATURES = {
         _i, [_vp, ctypes.c_int64, ctypes.c_char_p, _vp]),
     "paliwa_gb_transform_noalloc": (
         _i, [_vp, _i, _i, _pi64, _pi64, _pi64, _i, _i, _vp]),
+    "paliwa_gb_batch_use_slabs": (_i, [_vp, _i]),
+    "paliwa_gb_batch_status": (_i, [_vp]),
     "paliwa_gb_batch_create": (
         _i, [_i, _i, _pi64, _pi64, _pi64, _i, _i, ctypes.POINTER(_vp),
              ctypes.POINTER(_vp)]),

@@ -21,9 +21,18 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "combine.cuh"
 #include "paliwa_gb300.h"
 #include "plan.hpp"
+#include "slab.cuh"
+
+namespace pgb {
+void launch_slab_f64(int sched, SlabParams const &p, cudaStream_t s);
+void launch_slab_f32(int sched, SlabParams const &p, cudaStream_t s);
+void launch_slab_f32c(int sched, SlabParams const &p, cudaStream_t s);
+} // namespace pgb
 
 using namespace pgb;
 
@@ -33,6 +42,9 @@ namespace {
 // CT workload (3,025 grids, FP32c, forward + inverse): 28.7 ms with one
 // group, 26.1 with two, 25.7 with three, 25.6 with four.
 constexpr int kBatchGroups = 4;
+
+// Kernel code of a slab launch (slab.cuh); the others are plan.hpp's.
+constexpr int kSlab = 1024;
 
 struct Launch {
   int group = 0;
@@ -50,6 +62,7 @@ struct Direction {
   bool symmetric = true;
   std::vector<Launch> launches;
   LiftJob *jobs_dev = nullptr;
+  SlabJob *slab_dev = nullptr;  // jobs of the slab launches
   cudaGraphExec_t graph = nullptr;
   Tuning tuning;  // kernel forced per class (autotuner)
   // Classes of the plan's periodic stages: applicable kernels (bits), the
@@ -65,8 +78,10 @@ struct Direction {
 void free_direction(Direction &d) {
   if (d.graph) cudaGraphExecDestroy(d.graph);
   if (d.jobs_dev) cudaFree(d.jobs_dev);
+  if (d.slab_dev) cudaFree(d.slab_dev);
   d.graph = nullptr;
   d.jobs_dev = nullptr;
+  d.slab_dev = nullptr;
   d.launches.clear();
   d.classes.clear();
 }
@@ -119,9 +134,131 @@ struct paliwa_gb_batch {
   std::vector<size_t> group_shadow;
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> events;  // [0] fork, [k] join of group k
+  // Slab launches (slab.cuh): the tensor map over the grids' memory as
+  // 128-byte rows from slab_base, and the error word of their bounded waits.
+  bool use_slabs = true;
+  bool slab_map_ok = false;
+  unsigned long long slab_base = 0;
+  CUtensorMap slab_map{};
+  unsigned *slab_error = nullptr;
 };
 
 namespace {
+
+// The slab group of grid g: its trailing axes whose slab (the product of
+// their extents) fits one tile, when that group holds at least two axes
+// with levels to transform, the grid is a whole number of 1 KB boxes and
+// starts on a row of the tensor map. Returns the group's first axis, or
+// ndim for none.
+int slab_start(paliwa_gb_batch const &b, int g, int64_t const *levels,
+               int64_t const *lmin) {
+  size_t const es = dtype_size(b.dtype);
+  int const log2es = es == 8 ? 3 : 2;
+  int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
+  int64_t total = 0;
+  for (int d = 0; d < b.ndim; ++d) total += lv[d];
+  if (total + log2es < 10) return b.ndim;  // under one 1 KB box
+  unsigned long long const addr =
+      reinterpret_cast<unsigned long long>(b.grids[g]);
+  if (addr < b.slab_base || (addr - b.slab_base) % 128 != 0) return b.ndim;
+  int m = b.ndim;
+  int64_t vol = 0;
+  while (m > 0 && vol + lv[m - 1] + log2es <= 15) vol += lv[--m];
+  int work = 0;
+  for (int d = m; d < b.ndim; ++d) work += lv[d] > lmin[d];
+  return work >= 2 ? m : b.ndim;
+}
+
+// The slab job of grid g for its axes m..ndim-1: per axis with levels to
+// transform, the pencil length, its element stride inside a tile (the
+// product of the later extents) and the chunk size: 32 points (at most the
+// pencil) for the contiguous last axis and for strides of 32 elements or
+// more, 8 or fewer for smaller strides when the pencil's chunks then fit
+// the CTA's 256 threads (distinct shared-memory banks under the swizzle).
+SlabJob slab_job(paliwa_gb_batch const &b, int g, int m,
+                 int64_t const *levels, int64_t const *lmin,
+                 void *const *grid_ptrs) {
+  size_t const es = dtype_size(b.dtype);
+  int const log2es = es == 8 ? 3 : 2;
+  int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
+  SlabJob job;
+  std::memset(&job, 0, sizeof(job));
+  int64_t total = 0;
+  for (int d = 0; d < b.ndim; ++d) total += lv[d];
+  job.log2_tile = static_cast<int>(std::min<int64_t>(total, 15 - log2es));
+  job.row0 = static_cast<long long>(
+      (reinterpret_cast<unsigned long long>(grid_ptrs[g]) - b.slab_base) / 128);
+  int log2s = 0;
+  std::vector<SlabAxis> axes;
+  for (int d = b.ndim - 1; d >= m; --d) {
+    int const log2n = static_cast<int>(lv[d]);
+    int const nlev = static_cast<int>(lv[d] - lmin[d]);
+    if (nlev > 0) {
+      SlabAxis ax;
+      ax.log2n = static_cast<signed char>(log2n);
+      ax.log2s = static_cast<signed char>(log2s);
+      ax.nlevels = static_cast<signed char>(nlev);
+      int log2r = std::min(log2n, 5);
+      if (log2s >= 1 && log2s <= 4 && log2n + log2s - 3 <= 8)
+        log2r = std::min(log2n, 3);
+      ax.log2r = static_cast<signed char>(log2r);
+      axes.push_back(ax);
+    }
+    log2s += log2n;
+  }
+  std::reverse(axes.begin(), axes.end());
+  job.naxes = static_cast<int>(axes.size());
+  for (size_t i = 0; i < axes.size(); ++i) job.axis[i] = axes[i];
+  return job;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda): a 2D view [rows][128 bytes] from `base`, 1 KB boxes
+// (8 rows), 128-byte swizzle.
+bool encode_slab_map(CUtensorMap *map, unsigned long long base,
+                     unsigned long long rows, size_t es) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (encode == nullptr) {
+    cudaDriverEntryPointQueryResult q{};
+    void *fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                         cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || fn == nullptr)
+      return false;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if (rows == 0 || rows > (1ULL << 31)) return false;
+  cuuint64_t dims[2] = {static_cast<cuuint64_t>(128 / es), rows};
+  cuuint64_t strides[1] = {128};
+  cuuint32_t box[2] = {static_cast<cuuint32_t>(128 / es), 8};
+  cuuint32_t elem[2] = {1, 1};
+  CUresult const r = encode(
+      map, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                   : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+      2, reinterpret_cast<void *>(base), dims, strides, box, elem,
+      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// The tensor map over every grid of the batch (rows of 128 bytes from the
+// lowest grid address, rounded down to 128 bytes).
+void setup_slab_map(paliwa_gb_batch &b) {
+  b.slab_map_ok = false;
+  size_t const es = dtype_size(b.dtype);
+  unsigned long long lo = ~0ULL, hi = 0;
+  for (int g = 0; g < b.ngrids; ++g) {
+    unsigned long long const a = reinterpret_cast<unsigned long long>(b.grids[g]);
+    unsigned long long bytes = es;
+    for (int d = 0; d < b.ndim; ++d) bytes <<= b.levels[g * b.ndim + d];
+    lo = std::min(lo, a);
+    hi = std::max(hi, a + bytes);
+  }
+  lo &= ~127ULL;
+  b.slab_base = lo;
+  b.slab_map_ok = encode_slab_map(&b.slab_map, lo, (hi - lo + 127) / 128, es);
+}
 
 void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
                     int64_t const *levels, int64_t const *lmin,
@@ -131,7 +268,14 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
   dr.exact = exact_scalers(filters);
   dr.symmetric = symmetric_filters(filters);
   std::vector<LiftJob> all_jobs;
+  std::vector<SlabJob> all_slabs;
   size_t const es = dtype_size(b.dtype);
+  int const ws = wavelet_schedule(filters);
+  // First axis of every grid's slab group (ndim: none).
+  std::vector<int> slab_from(b.ngrids, b.ndim);
+  if (b.use_slabs && b.slab_map_ok && ws >= 0)
+    for (int g = 0; g < b.ngrids; ++g)
+      slab_from[g] = slab_start(b, g, levels, lmin);
   for (int grp = 0; grp < b.ngroups; ++grp) {
     std::vector<int> members;
     for (int g = 0; g < b.ngrids; ++g)
@@ -143,6 +287,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
       size_t shadow_off = b.group_shadow[grp];
       for (size_t i = 0; i < members.size(); ++i) {
         int const g = members[i];
+        if (d >= slab_from[g]) continue;  // in the grid's slab launch
         int64_t const *lv = levels + static_cast<size_t>(g) * b.ndim;
         AxisView view =
             axis_view(reinterpret_cast<unsigned long long>(grid_ptrs[g]),
@@ -180,7 +325,6 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
           Launch L;
           L.group = grp;
           L.R = R;
-          int const ws = wavelet_schedule(filters);
           L.sched = ws;
           for (Stage const *st : list)
             if (ws < 0 || !canonical_shifts(st->job, (ws & 1) != 0))
@@ -200,6 +344,31 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
         }
       }
     }
+    // The group's slab launch, after every per-axis stage of its grids.
+    Launch L;
+    L.group = grp;
+    L.R = kSlab;
+    L.sched = ws;
+    L.job_first = all_slabs.size();
+    for (int g : members) {
+      if (slab_from[g] >= b.ndim) continue;
+      SlabJob job = slab_job(b, g, slab_from[g], levels, lmin, grid_ptrs);
+      job.tile_begin = L.tiles;
+      int64_t total = 0;
+      for (int k = 0; k < b.ndim; ++k) total += levels[g * b.ndim + k];
+      L.tiles += 1LL << (total - job.log2_tile);
+      L.points += 1LL << total;
+      all_slabs.push_back(job);
+      ++L.njobs;
+    }
+    if (L.njobs > 0) dr.launches.push_back(L);
+  }
+  if (!all_slabs.empty()) {
+    size_t const bytes = all_slabs.size() * sizeof(SlabJob);
+    cuda_check(cudaMalloc(&dr.slab_dev, bytes), "cudaMalloc(slab jobs)");
+    cuda_check(cudaMemcpy(dr.slab_dev, all_slabs.data(), bytes,
+                          cudaMemcpyHostToDevice),
+               "cudaMemcpy(slab jobs)");
   }
   if (!all_jobs.empty()) {
     size_t const bytes = all_jobs.size() * sizeof(LiftJob);
@@ -208,6 +377,29 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
                           cudaMemcpyHostToDevice),
                "cudaMemcpy(jobs)");
   }
+}
+
+// One launch of a direction's plan: a lifting kernel or a slab kernel.
+void launch_one(paliwa_gb_batch &b, Direction &dr, Launch const &L,
+                cudaStream_t s) {
+  if (L.R != kSlab) {
+    launch_lift(b.dtype, dr.exact, dr.symmetric, L.sched, L.R, dr.params,
+                dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
+    return;
+  }
+  SlabParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.map = b.slab_map;
+  p.jobs = dr.slab_dev + L.job_first;
+  p.njobs = L.njobs;
+  p.total_tiles = L.tiles;
+  p.error = b.slab_error;
+  switch (b.dtype) {
+  case PALIWA_GB_F64: return launch_slab_f64(L.sched, p, s);
+  case PALIWA_GB_F32: return launch_slab_f32(L.sched, p, s);
+  case PALIWA_GB_F32C: return launch_slab_f32c(L.sched, p, s);
+  }
+  throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "unknown dtype");
 }
 
 void run_direction(paliwa_gb_batch &b, Direction &dr, cudaStream_t s) {
@@ -220,9 +412,7 @@ void run_direction(paliwa_gb_batch &b, Direction &dr, cudaStream_t s) {
       cuda_check(cudaStreamWaitEvent(b.streams[k - 1], b.events[0], 0),
                  "cudaStreamWaitEvent(fork)");
     for (auto const &L : dr.launches)
-      launch_lift(b.dtype, dr.exact, dr.symmetric, L.sched, L.R, dr.params,
-                  dr.jobs_dev + L.job_first, L.njobs, L.tiles,
-                  L.group == 0 ? s : b.streams[L.group - 1]);
+      launch_one(b, dr, L, L.group == 0 ? s : b.streams[L.group - 1]);
     for (int k = 1; k < b.ngroups; ++k) {
       cuda_check(cudaEventRecord(b.events[k], b.streams[k - 1]),
                  "cudaEventRecord(join)");
@@ -316,6 +506,7 @@ void setup_groups(paliwa_gb_batch &b, int want) {
   if (b.shadow) cudaFree(b.shadow);
   b.shadow = nullptr;
   assign_groups(b, b.levels.data(), b.lmin.data(), want);
+  setup_slab_map(b);
   if (b.shadow_bytes)
     cuda_check(cudaMalloc(&b.shadow, b.shadow_bytes), "cudaMalloc(shadow)");
   b.events.assign(b.ngroups, nullptr);
@@ -578,12 +769,17 @@ int paliwa_gb_batch_create(int ndim, int ngrids, const int64_t *levels,
       b->points += 1LL << total;
     }
     try {
+      cuda_check(cudaMalloc(&b->slab_error, sizeof(unsigned)),
+                 "cudaMalloc(error word)");
+      cuda_check(cudaMemset(b->slab_error, 0, sizeof(unsigned)),
+                 "cudaMemset(error word)");
       setup_groups(*b, kBatchGroups);
     } catch (...) {
       free_direction(b->dir[0]);
       free_direction(b->dir[1]);
       free_batch_streams(*b);
       if (b->shadow) cudaFree(b->shadow);
+      if (b->slab_error) cudaFree(b->slab_error);
       throw;
     }
     *out = b.release();
@@ -625,6 +821,34 @@ int paliwa_gb_batch_set_groups(paliwa_gb_batch *batch, int ngroups) {
   });
 }
 
+int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    batch->use_slabs = enable != 0;
+    setup_groups(*batch, batch->ngroups);
+  });
+}
+
+int paliwa_gb_batch_status(paliwa_gb_batch *batch) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    unsigned err = 0;
+    cuda_check(cudaMemcpy(&err, batch->slab_error, sizeof(err),
+                          cudaMemcpyDeviceToHost),
+               "cudaMemcpy(error word)");
+    if (err != 0) {
+      cuda_check(cudaMemset(batch->slab_error, 0, sizeof(err)),
+                 "cudaMemset(error word)");
+      throw StatusError(PALIWA_GB_TIMEOUT,
+                        "a slab kernel's bounded wait for its tile copy "
+                        "gave up");
+    }
+  });
+}
+
 int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
                          int64_t *launches_forward,
                          int64_t *launches_inverse) {
@@ -651,9 +875,7 @@ float time_direction(paliwa_gb_batch &b, int which, int reps,
   cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
   cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
   auto run = [&](Direction &dr) {
-    for (auto const &L : dr.launches)
-      launch_lift(b.dtype, dr.exact, dr.symmetric, L.sched, L.R, dr.params,
-                  dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
+    for (auto const &L : dr.launches) launch_one(b, dr, L, s);
   };
   float best = 1e30f;
   for (int r = 0; r < reps; ++r) {
@@ -768,8 +990,7 @@ int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
     cuda_check(cudaEventRecord(ev[0], s), "cudaEventRecord");
     for (int i = 0; i < n; ++i) {
       Launch const &L = dr.launches[i];
-      launch_lift(batch->dtype, dr.exact, dr.symmetric, L.sched, L.R,
-                  dr.params, dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
+      launch_one(*batch, dr, L, s);
       cuda_check(cudaEventRecord(ev[i + 1], s), "cudaEventRecord");
       bytes[i] = static_cast<int64_t>(2 * es) * L.points;
       if (kernels != nullptr) kernels[i] = L.R;
@@ -788,6 +1009,7 @@ void paliwa_gb_batch_destroy(paliwa_gb_batch *batch) {
   free_direction(batch->dir[1]);
   free_batch_streams(*batch);
   if (batch->shadow) cudaFree(batch->shadow);
+  if (batch->slab_error) cudaFree(batch->slab_error);
   delete batch;
 }
 

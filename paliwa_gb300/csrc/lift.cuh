@@ -208,6 +208,9 @@ __device__ __forceinline__ int tile_pitch(int G, int log2_inner,
 // per tile).
 template <class A, int NT> struct RoundCtx {
   using V = typename A::V;
+  // Chunk heads of one column are consecutive threads (coarse_heads may
+  // run a column's coarse levels as a pencil of heads in one warp).
+  static constexpr bool kHeadPencil = true;
   int t, c, G, log2G, log2ls, gbase_lane, periodic;
   V *heads, *xch;
   int buf = 0;
@@ -279,9 +282,9 @@ template <class A, int NT> struct RoundCtx {
 // Schedule for arbitrary level lists and filters (transform_in): levels,
 // parities and coefficients are read per step.
 struct RuntimeSched {
-  template <class A, int R, int NT>
+  template <class A, int R, int NT, class Ctx>
   static __device__ __forceinline__ void run(typename A::V (&v)[R],
-                                             RoundCtx<A, NT> &ctx,
+                                             Ctx &ctx,
                                              LiftJob const &job,
                                              LiftParams const &p) {
     using V = typename A::V;
@@ -352,9 +355,9 @@ template <> struct WaveletPasses<2, false> {
 template <int W, bool FWD> struct WaveletSched {
   using Passes = typename WaveletPasses<W, FWD>::type;
 
-  template <class A, int R, int NT, int K, class P>
+  template <class A, int R, int NT, int K, class P, class Ctx>
   static __device__ __forceinline__ void fine_pass(typename A::V (&v)[R],
-                                                   RoundCtx<A, NT> &ctx) {
+                                                   Ctx &ctx) {
     using V = typename A::V;
     constexpr int S = 1 << K;
     constexpr Coeffs cf = P::coeffs();
@@ -376,16 +379,16 @@ template <int W, bool FWD> struct WaveletSched {
     ctx.fine_wrote_heads(P::offset);
   }
 
-  template <class A, int R, int NT, int K, class... P>
+  template <class A, int R, int NT, int K, class... P, class Ctx>
   static __device__ __forceinline__ void fine_level(typename A::V (&v)[R],
-                                                    RoundCtx<A, NT> &ctx,
+                                                    Ctx &ctx,
                                                     PassList<P...>) {
     (fine_pass<A, R, NT, K, P>(v, ctx), ...);
   }
 
-  template <class A, int R, int NT, class... P>
+  template <class A, int R, int NT, class... P, class Ctx>
   static __device__ __forceinline__ void coarse_level(typename A::V (&v)[R],
-                                                      RoundCtx<A, NT> &ctx,
+                                                      Ctx &ctx,
                                                       int d, PassList<P...>) {
     using V = typename A::V;
     (ctx.coarse(v[0], P::offset, d,
@@ -396,9 +399,9 @@ template <int W, bool FWD> struct WaveletSched {
      ...);
   }
 
-  template <class A, int R, int NT, int K>
+  template <class A, int R, int NT, int K, class Ctx>
   static __device__ __forceinline__ void fine_up(typename A::V (&v)[R],
-                                                 RoundCtx<A, NT> &ctx, int L) {
+                                                 Ctx &ctx, int L) {
     if constexpr ((1 << K) < R) {
       if (K < L) {
         fine_level<A, R, NT, K>(v, ctx, Passes{});
@@ -406,9 +409,9 @@ template <int W, bool FWD> struct WaveletSched {
       }
     }
   }
-  template <class A, int R, int NT, int K>
+  template <class A, int R, int NT, int K, class Ctx>
   static __device__ __forceinline__ void fine_down(typename A::V (&v)[R],
-                                                   RoundCtx<A, NT> &ctx,
+                                                   Ctx &ctx,
                                                    int L) {
     if constexpr (K >= 0) {
       if (K < L) fine_level<A, R, NT, K>(v, ctx, Passes{});
@@ -419,9 +422,9 @@ template <int W, bool FWD> struct WaveletSched {
   // ---- packed variant (A::kPacked): registers hold pairs (slot x,
   // slot x + R/2) so that fine steps of distance <= R/4 update two points
   // per f32x2 instruction.
-  template <class A, int R, int NT, int K, class P>
+  template <class A, int R, int NT, int K, class P, class Ctx>
   static __device__ __forceinline__ void fine_pass_packed(DF2 (&q)[R / 2],
-                                                          RoundCtx<A, NT> &ctx) {
+                                                          Ctx &ctx) {
     using V = typename A::V;
     constexpr int H = R / 2;
     constexpr int S = 1 << K;
@@ -470,14 +473,14 @@ template <int W, bool FWD> struct WaveletSched {
     }
   }
 
-  template <class A, int R, int NT, int K, class... P>
+  template <class A, int R, int NT, int K, class... P, class Ctx>
   static __device__ __forceinline__ void fine_level_packed(
-      DF2 (&q)[R / 2], RoundCtx<A, NT> &ctx, PassList<P...>) {
+      DF2 (&q)[R / 2], Ctx &ctx, PassList<P...>) {
     (fine_pass_packed<A, R, NT, K, P>(q, ctx), ...);
   }
-  template <class A, int R, int NT, int K>
+  template <class A, int R, int NT, int K, class Ctx>
   static __device__ __forceinline__ void fine_up_packed(DF2 (&q)[R / 2],
-                                                        RoundCtx<A, NT> &ctx,
+                                                        Ctx &ctx,
                                                         int L) {
     if constexpr ((1 << K) < R) {
       if (K < L) {
@@ -486,18 +489,18 @@ template <int W, bool FWD> struct WaveletSched {
       }
     }
   }
-  template <class A, int R, int NT, int K>
+  template <class A, int R, int NT, int K, class Ctx>
   static __device__ __forceinline__ void fine_down_packed(
-      DF2 (&q)[R / 2], RoundCtx<A, NT> &ctx, int L) {
+      DF2 (&q)[R / 2], Ctx &ctx, int L) {
     if constexpr (K >= 0) {
       if (K < L) fine_level_packed<A, R, NT, K>(q, ctx, Passes{});
       fine_down_packed<A, R, NT, K - 1>(q, ctx, L);
     }
   }
   // Coarse levels act on slot 0 only: unpack it, run them, pack it back.
-  template <class A, int R, int NT>
+  template <class A, int R, int NT, class Ctx>
   static __device__ __forceinline__ void coarse_packed(DF2 (&q)[R / 2],
-                                                       RoundCtx<A, NT> &ctx,
+                                                       Ctx &ctx,
                                                        int sh_first,
                                                        int sh_last, int step) {
     using V = typename A::V;
@@ -536,11 +539,11 @@ template <int W, bool FWD> struct WaveletSched {
 #pragma unroll
     for (int k = 0; k < K; ++k) col[lane * K + k] = hv[k];
   }
-  template <class A, int R, int NT>
+  template <class A, int R, int NT, class Ctx>
   static __device__ __forceinline__ bool coarse_heads(typename A::V &head,
-                                                      RoundCtx<A, NT> &ctx,
+                                                      Ctx &ctx,
                                                       int Lc) {
-    if constexpr (R < 16) {
+    if constexpr (R < 16 || !Ctx::kHeadPencil) {
       return false;
     } else {
       if (ctx.G <= 32 || ctx.G > 256) return false;
@@ -564,18 +567,18 @@ template <int W, bool FWD> struct WaveletSched {
     }
   }
 
-  template <class A, int R, int NT>
+  template <class A, int R, int NT, class Ctx>
   static __device__ __forceinline__ void run(typename A::V (&v)[R],
-                                             RoundCtx<A, NT> &ctx,
+                                             Ctx &ctx,
                                              LiftJob const &job,
                                              LiftParams const &) {
     run_levels<A, R, NT>(v, ctx, job.nlevels);
   }
 
   // The L levels of a job (shifts 0 .. L-1 forward, L-1 .. 0 inverse).
-  template <class A, int R, int NT>
+  template <class A, int R, int NT, class Ctx>
   static __device__ __forceinline__ void run_levels(typename A::V (&v)[R],
-                                                    RoundCtx<A, NT> &ctx,
+                                                    Ctx &ctx,
                                                     int L) {
     constexpr int LOG2R = Log2<R>::value;
     if constexpr (A::kPacked && R >= 4) {

@@ -1,0 +1,9 @@
+// Slab kernel instantiations for one arithmetic policy (compiled apart so
+// that the library builds in parallel).
+#include "slab_launch.cuh"
+
+namespace pgb {
+void launch_slab_f32c(int sched, SlabParams const &p, cudaStream_t s) {
+  launch_slab_any<CompensatedT<true>>(sched, p, s);
+}
+} // namespace pgb

@@ -70,6 +70,8 @@ def packed_grids(levels, dtype, device="cuda", align=64):
 
 def kernel_name(code):
     """Name of the lifting kernel behind a launch code of Batch.profile."""
+    if code == 1024:
+        return "slab_kernel"
     if code == 512:
         return "copy_kernel"
     if code > 256:
@@ -114,7 +116,8 @@ class Batch:
     parallel branches (see :meth:`set_groups`)."""
 
     def __init__(self, grids, levels, minimum_level, maximum_level,
-                 wavelet_name="hat", compensated=False, groups=None):
+                 wavelet_name="hat", compensated=False, groups=None,
+                 slabs=True):
         _check_grids(grids, levels)
         self.grids = list(grids)
         self.levels = [tuple(int(x) for x in l) for l in levels]
@@ -128,8 +131,21 @@ class Batch:
             wavelet_id(wavelet_name), _ptr_array(grids),
             ctypes.byref(self._h)))
         self.points = sum(g.numel() for g in grids)
+        if not slabs:
+            self.use_slabs(False)
         if groups is not None:
             self.set_groups(groups)
+
+    def use_slabs(self, enable):
+        """Plan the trailing axes of grids whose slabs fit a tile as one
+        slab launch (default), or every axis on its own (the same bits).
+        Synchronizes the device."""
+        _lib.check(self._lib.paliwa_gb_batch_use_slabs(self._h, int(enable)))
+
+    def status(self):
+        """Raises DeviceTimeout if a slab launch gave up a bounded wait for
+        its tile copies since the last call. Synchronizes the device."""
+        _lib.check(self._lib.paliwa_gb_batch_status(self._h))
 
     def set_groups(self, ngroups):
         """Split the grids into ``ngroups`` groups of about equal size, each

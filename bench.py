@@ -36,8 +36,9 @@ workload ("replicas only"); value sums the ranks' points over the slowest
 rank's time.
 
 ``--probe-axis LEVELS:DIM:MODE`` instead times one axis of one random grid,
-``--probe-outputs LEVELS:DIM:MODE`` the restricted-output transform of one
-(both used for single-kernel captures).
+``--probe-outputs LEVELS:DIM:MODE`` the restricted-output transform of one,
+``--probe-batch LEVEL_SUM:MODE`` one direction of a smaller 4D batch launch
+by launch (all three used for single-kernel captures).
 """
 from __future__ import annotations
 
@@ -329,7 +330,7 @@ def run_reference(args, w, world, rank):
 # GPU
 
 
-DRAM_RATIO_FILE = "profiles/lift_kernels_4d_ct_20_dram_ratio.txt"
+DRAM_RATIO_FILE = "profiles/dram_ratio_4d_ct_19.txt"
 # Groups of grids whose host copies overlap each other's transforms in the
 # end-to-end measurement.
 E2E_GROUPS = 32
@@ -338,8 +339,11 @@ E2E_COPY_STREAMS = 1
 
 def dram_ratio(kernel):
     """DRAM bytes per algorithmic byte of `kernel` (a name of
-    paliwa_gb300.ct.kernel_name) as measured by ncu on the 4d-ct-20 workload
-    and committed as 'name = ratio' lines; None when not measured."""
+    paliwa_gb300.ct.kernel_name), measured by ncu on single-kernel captures
+    of the 4D combination batch at |l|_1 = 19 - q (``--probe-batch 19:f32c``,
+    2.8 GB on the device, three launches per kernel) and committed as
+    'name = ratio' lines; None when not measured. The ratio of a launch's DRAM bytes to the bytes it must move does not
+    depend on the number of grids, so it scales to the full workload."""
     path = os.path.join(ROOT, DRAM_RATIO_FILE)
     if not os.path.exists(path):
         return None
@@ -622,6 +626,7 @@ def run_gpu(args, w, world, rank, local):
         os.sched_setaffinity(0, saved)
     host_in.copy_(b32)
     del b32, v32
+    link = measure_link(host_in, host_out, hb.buf)
 
     def e2e_step():
         hb.run(host_in, host_out, stream=stream)
@@ -632,6 +637,11 @@ def run_gpu(args, w, world, rank, local):
     e2e_ms = max_over_ranks(world, e2e_ms)
     e2e_value = pts_step * max(1, args.steps // 2) / (e2e_ms / 1e3)
     e2e_bytes = hb.numel() * 4
+    # The host link in this run: each direction moves e2e_bytes per step,
+    # both at once; the fraction compares that with the concurrent rate.
+    e2e_each = e2e_bytes / (e2e_ms / 1e3 / max(1, args.steps // 2)) / 1e9
+    link["e2e_gbs_each_direction"] = e2e_each
+    link["link_frac"] = e2e_each / link["concurrent_gbs_each"]
     hb.close()
 
     cpu = None
@@ -663,9 +673,11 @@ def run_gpu(args, w, world, rank, local):
                 "bound": "hbm", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "traffic_source": None if ratio is None else
-                    "DRAM bytes / algorithmic bytes of this kernel from the "
-                    "ncu capture in " + DRAM_RATIO_FILE + ", times this "
-                    "run's algorithmic bytes per launch",
+                    "DRAM bytes / algorithmic bytes of this kernel from "
+                    "single-kernel ncu captures of the 4D batch at |l|_1 = "
+                    "19 - q in "
+                    + DRAM_RATIO_FILE + ", times this run's bytes per "
+                    "launch",
                 "peak_kind": peak_kind,
                 "kernel": top_name + ", FP32c (largest share of the step)",
                 "launches_per_step": top_n,
@@ -682,6 +694,12 @@ def run_gpu(args, w, world, rank, local):
                 # there; all_launches_frac times them one by one).
                 "step_bytes": step_bytes(w, 4),
                 "step_frac": step_bytes(w, 4) /
+                    (ms32 / args.steps / 1e3) / 1e9 / peak,
+                # The plan's own HBM traffic (a slab launch reads and
+                # writes each point once for all of its axes): the sum of
+                # the launches' bytes over the graph-timed step.
+                "step_plan_bytes": tot32_b,
+                "step_plan_frac": tot32_b /
                     (ms32 / args.steps / 1e3) / 1e9 / peak},
             "combine": combine,
             "autotune": tuning,
@@ -689,13 +707,49 @@ def run_gpu(args, w, world, rank, local):
             "e2e": {"value": e2e_value, "unit": "points/s",
                     "h2d_bytes_per_step": e2e_bytes,
                     "d2h_bytes_per_step": e2e_bytes,
-                    "groups": E2E_GROUPS, "host_numa_node": numa},
+                    "groups": E2E_GROUPS, "host_numa_node": numa,
+                    "link": link},
             "gpu_launches": args.steps * nlaunch,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
     bt32.close()
     bt64.close()
+
+
+def measure_link(host_in, host_out, dev_buf):
+    """GB/s of the host link in this run: the whole pinned input copied to
+    the device, the device buffer copied to the pinned output, and both at
+    once on two streams (each direction's rate), best of two, CUDA events."""
+    import torch
+    nbytes = dev_buf.numel() * dev_buf.element_size()
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+    def once(h2d, d2h):
+        torch.cuda.synchronize()
+        ev[0].record(s_in)
+        s_out.wait_event(ev[0])
+        if h2d:
+            with torch.cuda.stream(s_in):
+                dev_buf.copy_(host_in, non_blocking=True)
+        ev[1].record(s_in)
+        ev[2].record(s_out)
+        if d2h:
+            with torch.cuda.stream(s_out):
+                host_out.copy_(dev_buf, non_blocking=True)
+        ev[3].record(s_out)
+        torch.cuda.synchronize()
+        if h2d and d2h:
+            return max(ev[0].elapsed_time(ev[1]), ev[0].elapsed_time(ev[3]))
+        return ev[0].elapsed_time(ev[1] if h2d else ev[3])
+
+    out = {}
+    for key, h2d, d2h in (("h2d_gbs", True, False), ("d2h_gbs", False, True),
+                          ("concurrent_gbs_each", True, True)):
+        ms = min(once(h2d, d2h) for _ in range(2))
+        out[key] = nbytes / (ms / 1e3) / 1e9
+    return out
 
 
 def run_axis_probe(spec):
@@ -723,6 +777,37 @@ def run_axis_probe(spec):
     ms = ev[0].elapsed_time(ev[1])
     gbs = 2 * g.numel() * g.element_size() / ms / 1e6
     print(json.dumps({"probe": spec, "ms": ms, "GB/s": gbs}), flush=True)
+
+
+def run_batch_probe(spec):
+    """One direction of a smaller 4D combination batch, for kernel captures
+    of a few GB: ``LEVEL_SUM:MODE[:noslabs]`` (MODE f64, f32 or f32c; e.g.
+    ``19:f32c``, 709 M points, 2.8 GB) builds the 4D scheme at |l|_1 =
+    LEVEL_SUM - q (q <= 3, lmin 1, CDF biorthogonal) on random values with
+    the planner's default kernels, runs the forward direction launch by
+    launch (no graph, plan order, one stream) and prints one JSON line per
+    launch: index, kernel, algorithmic bytes and event-timed milliseconds.
+    The k-th launch of a kernel in that list is the k-th one a profiler
+    filtered on the kernel's name sees."""
+    import torch
+
+    from paliwa_gb300 import ct as pct
+    parts = spec.split(":")
+    level_sum, mode = int(parts[0]), parts[1]
+    slabs = not (len(parts) > 2 and parts[2] == "noslabs")
+    levels, _ = pct.combination_scheme(4, level_sum, 3, 1)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    buf, views = pct.packed_grids(levels, dt)
+    buf.uniform_(-1, 1)
+    top = level_sum - 3
+    bt = pct.Batch(views, levels, (1,) * 4, (top,) * 4, "biorthogonal",
+                   compensated=(mode == "f32c"), slabs=slabs)
+    ms, by, kd = bt.profile(forward=True)
+    bt.status()
+    for i, (m, b, k) in enumerate(zip(ms, by, kd)):
+        print(json.dumps({"launch": i, "kernel": pct.kernel_name(k),
+                          "bytes": b, "ms": m}), flush=True)
+    bt.close()
 
 
 def run_outputs_probe(spec):
@@ -794,7 +879,14 @@ def main():
     ap.add_argument("--probe-outputs", metavar="LEVELS:DIM:MODE",
                     help="time the restricted-output transform of one grid "
                          "(outputs: half the axis), e.g. 10,8,8:0:f64")
+    ap.add_argument("--probe-batch", metavar="LEVEL_SUM:MODE[:noslabs]",
+                    help="profile one direction of the 4D combination batch "
+                         "at a smaller level sum launch by launch (for "
+                         "kernel captures), e.g. 19:f32c")
     args = ap.parse_args()
+    if args.probe_batch:
+        run_batch_probe(args.probe_batch)
+        return
     if args.probe_axis:
         run_axis_probe(args.probe_axis)
         return

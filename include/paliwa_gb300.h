@@ -278,8 +278,11 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,
                             int64_t *bytes, int32_t *kernels);
-/* Autotuner: for each direction, each class of periodic stages (last axis
- * or strided, sub-lattice or not, pencil length, inner extent) and each
+/* Autotuner: for each direction, first slab launches against the same
+ * axes planned one by one (when paliwa_gb_batch_use_slabs allows slabs;
+ * either way round, the faster kept), then each class of periodic stages
+ * (last axis or strided, sub-lattice or not, pencil length, inner extent)
+ * and each
  * kernel that applies to it (staged, direct, wide, tile), re-plans and times
  * the whole direction (best of `reps` event-timed runs without a graph) and
  * keeps the fastest choice; classes are tried one after another (coordinate
@@ -288,7 +291,8 @@ int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
  * grids: every timed direction is paired with its inverse, so the contents
  * come back up to rounding (bit-exact for FP64 and FP32 only if the
  * transform pair is exact on them). Synchronises with the stream. *changed
- * (may be null) = classes whose kernel changed. Takes a second or more for
+ * (may be null) = classes whose kernel changed, plus directions whose slab
+ * choice changed. Takes a second or more for
  * a large batch; graphs are re-captured on the next run. No counterpart in
  * the reference, which has no kernel choice to make. */
 int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,

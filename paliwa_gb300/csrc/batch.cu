@@ -65,6 +65,9 @@ struct Direction {
   SlabJob *slab_dev = nullptr;  // jobs of the slab launches
   cudaGraphExec_t graph = nullptr;
   Tuning tuning;  // kernel forced per class (autotuner)
+  // Slab launches where they apply (the batch's setting); the autotuner
+  // clears it when the direction runs faster axis by axis.
+  bool slabs = true;
   // Classes of the plan's periodic stages: applicable kernels (bits), the
   // default choice of the first stage seen, and the points they store.
   struct ClassInfo {
@@ -273,7 +276,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
   int const ws = wavelet_schedule(filters);
   // First axis of every grid's slab group (ndim: none).
   std::vector<int> slab_from(b.ngrids, b.ndim);
-  if (b.use_slabs && b.slab_map_ok && ws >= 0)
+  if (b.use_slabs && dr.slabs && b.slab_map_ok && ws >= 0)
     for (int g = 0; g < b.ngrids; ++g)
       slab_from[g] = slab_start(b, g, levels, lmin);
   for (int grp = 0; grp < b.ngroups; ++grp) {
@@ -913,12 +916,28 @@ int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,
     int nchanged = 0;
     for (int which = 0; which < 2; ++which) {
       Direction &dr = batch->dir[which];
+      float best = time_direction(*batch, which, reps, s);
+      // Slab launches against the same axes planned one by one (either way
+      // round, so that a second call can bring the slabs back).
+      bool has_slab = false;
+      for (auto const &L : dr.launches) has_slab |= L.R == kSlab;
+      if (batch->use_slabs && batch->slab_map_ok && (has_slab || !dr.slabs)) {
+        dr.slabs = !dr.slabs;
+        replan(*batch, which);
+        float const t = time_direction(*batch, which, reps, s);
+        if (t < best * 0.99f) {
+          best = t;
+          ++nchanged;
+        } else {
+          dr.slabs = !dr.slabs;
+          replan(*batch, which);
+        }
+      }
       // Coordinate descent over the classes of periodic stages: try every
       // kernel that applies to a class, keep the fastest whole direction.
       auto const classes = dr.classes;
       long long total = 0;
       for (auto const &kv : classes) total += kv.second.points;
-      float best = time_direction(*batch, which, reps, s);
       for (auto const &[tclass, info] : classes) {
         unsigned const mask = info.kernels;
         int const dflt = info.dflt;

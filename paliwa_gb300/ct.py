@@ -68,9 +68,13 @@ def packed_grids(levels, dtype, device="cuda", align=64):
     return buf, [buf.narrow(0, o, s) for o, s in zip(offsets, sizes)]
 
 
+# Launch code of the slab kernel in Batch.profile.
+SLAB_KERNEL = 1024
+
+
 def kernel_name(code):
     """Name of the lifting kernel behind a launch code of Batch.profile."""
-    if code == 1024:
+    if code == SLAB_KERNEL:
         return "slab_kernel"
     if code == 512:
         return "copy_kernel"

@@ -44,7 +44,6 @@ def run_pair(levels, lmin, lmax, wavelet, dtype, compensated, seed):
         s = torch.cuda.Stream()
         bt = pct.Batch(views, levels, lmin, lmax, wavelet,
                        compensated=compensated, slabs=slabs)
-        fwd, inv = bt.launches()
         bt.hierarchize(s)
         s.synchronize()
         f = buf.clone()
@@ -53,7 +52,13 @@ def run_pair(levels, lmin, lmax, wavelet, dtype, compensated, seed):
         bt.status()
         esz = buf.element_size()
         starts = [(v.data_ptr() - buf.data_ptr()) // esz for v in views]
-        out.append((f, buf.clone(), starts, fwd))
+        out.append((f, buf.clone(), starts))
+        # The kernels of the forward plan (this runs it once more, after
+        # the results were taken).
+        _, _, kernels = bt.profile(forward=True, stream=s)
+        s.synchronize()
+        bt.status()
+        out[-1] += (kernels,)
         bt.close()
     return host, out
 
@@ -68,10 +73,10 @@ def test_slab_plan_equals_per_axis_plan(dtype_name, case):
     lmin, lmax = (1,) * ndim, (top,) * ndim
     dtype = torch.float64 if dtype_name == "f64" else torch.float32
     for w, wavelet in enumerate(WAVELETS):
-        host, ((f1, b1, v1, n1), (f2, b2, _, n2)) = run_pair(
+        host, ((f1, b1, v1, k1), (f2, b2, _, k2)) = run_pair(
             levels, lmin, lmax, wavelet, dtype, dtype_name == "f32c",
             100 * ndim + top + w)
-        assert n1 < n2  # the slab plan has fewer launches
+        assert pct.SLAB_KERNEL in k1 and pct.SLAB_KERNEL not in k2
         assert torch.equal(f1, f2), (case, wavelet)
         assert torch.equal(b1, b2), (case, wavelet)
         if dtype_name == "f64" and w == 1:
@@ -94,7 +99,8 @@ def test_slab_lmin_zero_and_single_tile_grids():
               (2, 2, 4), (4, 6, 2), (1, 7, 7)]
     lmin, lmax = (0, 0, 0), (7, 7, 7)
     for dtype, comp in ((torch.float64, False), (torch.float32, True)):
-        host, ((f1, b1, _, _), (f2, b2, _, _)) = run_pair(
+        host, ((f1, b1, _, k1), (f2, b2, _, _)) = run_pair(
             levels, lmin, lmax, "biorthogonal", dtype, comp, 5)
+        assert pct.SLAB_KERNEL in k1
         assert torch.equal(f1, f2)
         assert torch.equal(b1, b2)

@@ -689,7 +689,7 @@ def run_gpu(args, w, world, rank, local):
                 # The step itself: its algorithmic bytes (one read and one
                 # write of every point per transformed axis and direction;
                 # axes at the minimum level have no levels and move
-                # nothing; the long pencils' copy stages are not counted)
+                # nothing; the long pencils' halo passes are not counted)
                 # over the graph-timed step (the groups' launches overlap
                 # there; all_launches_frac times them one by one).
                 "step_bytes": step_bytes(w, 4),

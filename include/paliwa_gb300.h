@@ -255,6 +255,12 @@ int paliwa_gb_batch_set_groups(paliwa_gb_batch *batch, int ngroups);
  * directions after synchronizing the device. No counterpart in the
  * reference. */
 int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable);
+/* ctas > 0 caps every launch of the batch at that many CTAs per SM (the
+ * kernels are persistent: by default a launch takes every slot that fits),
+ * which leaves room on each SM for the launches of the batch's other
+ * groups; 0 (default) restores the default. Re-plans both directions after
+ * synchronizing the device. No counterpart in the reference. */
+int paliwa_gb_batch_set_ctas_per_sm(paliwa_gb_batch *batch, int ctas);
 /* PALIWA_GB_TIMEOUT if a slab launch of this batch gave up a bounded wait
  * for its tile copies since the last call (the flag is then cleared);
  * otherwise PALIWA_GB_OK. Synchronizes with the device. */
@@ -270,8 +276,9 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
  * kernel (rows of adjacent columns in registers) on a strided axis and on
  * the last axis, 192 + R and 256 + R the tile kernel (row-major tiles in
  * shared memory, rows of adjacent columns in registers) for pencils of up to
- * 32 chunks and longer ones, 512 the flat copy of windowed stages' results
- * back into the grids, 1024 the slab kernel (every level of a grid's
+ * 32 chunks and longer ones, 512 the halo pass before a windowed stage
+ * (its bytes count one read and one write of each point it copies), 1024
+ * the slab kernel (every level of a grid's
  * trailing axes in one pass; its bytes count one read and one write of each
  * point); `kernels` may be null. Call with
  * capacity 0 to get *nlaunches first. */

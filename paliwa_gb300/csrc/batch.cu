@@ -51,6 +51,7 @@ struct Launch {
   int R = 0;
   int sched = -1;
   size_t job_first = 0;  // index into the device job array
+  size_t tile_first = 0;  // slab launches: index into the tile-job table
   int njobs = 0;
   long long tiles = 0;
   long long points = 0;  // grid points stored by this launch
@@ -63,6 +64,7 @@ struct Direction {
   std::vector<Launch> launches;
   LiftJob *jobs_dev = nullptr;
   SlabJob *slab_dev = nullptr;  // jobs of the slab launches
+  int *slab_tile_dev = nullptr;  // job of every tile of the slab launches
   cudaGraphExec_t graph = nullptr;
   Tuning tuning;  // kernel forced per class (autotuner)
   // Slab launches where they apply (the batch's setting); the autotuner
@@ -82,6 +84,8 @@ void free_direction(Direction &d) {
   if (d.graph) cudaGraphExecDestroy(d.graph);
   if (d.jobs_dev) cudaFree(d.jobs_dev);
   if (d.slab_dev) cudaFree(d.slab_dev);
+  if (d.slab_tile_dev) cudaFree(d.slab_tile_dev);
+  d.slab_tile_dev = nullptr;
   d.graph = nullptr;
   d.jobs_dev = nullptr;
   d.slab_dev = nullptr;
@@ -144,6 +148,8 @@ struct paliwa_gb_batch {
   unsigned long long slab_base = 0;
   CUtensorMap slab_map{};
   unsigned *slab_error = nullptr;
+  // Cap on the CTAs per SM of every launch (0: as many as fit).
+  int ctas_per_sm = 0;
 };
 
 namespace {
@@ -272,6 +278,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
   dr.symmetric = symmetric_filters(filters);
   std::vector<LiftJob> all_jobs;
   std::vector<SlabJob> all_slabs;
+  std::vector<int> slab_tiles;  // per slab launch tile: its job in the launch
   size_t const es = dtype_size(b.dtype);
   int const ws = wavelet_schedule(filters);
   // First axis of every grid's slab group (ndim: none).
@@ -338,9 +345,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
             LiftJob job = st->job;
             job.tile_begin = L.tiles;
             L.tiles += st->tiles;
-            L.points += st->R == kCopy
-                            ? st->job.columns / static_cast<long long>(es)
-                            : st->job.columns << st->job.log2_n;
+            L.points += stage_points(*st);
             all_jobs.push_back(job);
           }
           if (L.R != 0 && L.tiles > 0) dr.launches.push_back(L);
@@ -353,13 +358,16 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
     L.R = kSlab;
     L.sched = ws;
     L.job_first = all_slabs.size();
+    L.tile_first = slab_tiles.size();
     for (int g : members) {
       if (slab_from[g] >= b.ndim) continue;
       SlabJob job = slab_job(b, g, slab_from[g], levels, lmin, grid_ptrs);
       job.tile_begin = L.tiles;
       int64_t total = 0;
       for (int k = 0; k < b.ndim; ++k) total += levels[g * b.ndim + k];
-      L.tiles += 1LL << (total - job.log2_tile);
+      long long const tiles = 1LL << (total - job.log2_tile);
+      slab_tiles.insert(slab_tiles.end(), tiles, L.njobs);
+      L.tiles += tiles;
       L.points += 1LL << total;
       all_slabs.push_back(job);
       ++L.njobs;
@@ -372,6 +380,12 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
     cuda_check(cudaMemcpy(dr.slab_dev, all_slabs.data(), bytes,
                           cudaMemcpyHostToDevice),
                "cudaMemcpy(slab jobs)");
+    size_t const tbytes = slab_tiles.size() * sizeof(int);
+    cuda_check(cudaMalloc(&dr.slab_tile_dev, tbytes),
+               "cudaMalloc(slab tiles)");
+    cuda_check(cudaMemcpy(dr.slab_tile_dev, slab_tiles.data(), tbytes,
+                          cudaMemcpyHostToDevice),
+               "cudaMemcpy(slab tiles)");
   }
   if (!all_jobs.empty()) {
     size_t const bytes = all_jobs.size() * sizeof(LiftJob);
@@ -386,14 +400,18 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
 void launch_one(paliwa_gb_batch &b, Direction &dr, Launch const &L,
                 cudaStream_t s) {
   if (L.R != kSlab) {
-    launch_lift(b.dtype, dr.exact, dr.symmetric, L.sched, L.R, dr.params,
+    LiftParams lp = dr.params;
+    lp.ctas_per_sm = b.ctas_per_sm;
+    launch_lift(b.dtype, dr.exact, dr.symmetric, L.sched, L.R, lp,
                 dr.jobs_dev + L.job_first, L.njobs, L.tiles, s);
     return;
   }
   SlabParams p;
   std::memset(&p, 0, sizeof(p));
+  p.ctas_per_sm = b.ctas_per_sm;
   p.map = b.slab_map;
   p.jobs = dr.slab_dev + L.job_first;
+  p.tile_job = dr.slab_tile_dev + L.tile_first;
   p.njobs = L.njobs;
   p.total_tiles = L.tiles;
   p.error = b.slab_error;
@@ -830,6 +848,17 @@ int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable) {
       throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
     cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
     batch->use_slabs = enable != 0;
+    setup_groups(*batch, batch->ngroups);
+  });
+}
+
+int paliwa_gb_batch_set_ctas_per_sm(paliwa_gb_batch *batch, int ctas) {
+  return guarded([&] {
+    if (batch == nullptr || ctas < 0)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                        "null batch or negative CTA count");
+    cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    batch->ctas_per_sm = ctas;
     setup_groups(*batch, batch->ngroups);
   });
 }

@@ -140,10 +140,6 @@ LiftParams launch_params(std::vector<Filter> const &filters) {
   LiftParams p;
   std::memset(&p, 0, sizeof(p));
   p.npasses = static_cast<int>(filters.size());
-  // Per-pencil FP64 steps run as whole warp instructions on GB300's FP64
-  // pipe even when only one lane is active; measured, they cost more than
-  // the rest of the FP32-compensated transform. The coarsest levels
-  // therefore stay in double-float arithmetic unless enabled here.
   for (size_t i = 0; i < filters.size(); ++i) {
     if (filters[i].offset != 0 && filters[i].offset != 1)
       throw StatusError(PALIWA_GB_RUNTIME_ERROR, "Filter offset not supported");
@@ -332,43 +328,45 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
                         "filter list too long for windowed long pencils");
     if (v.shadow == 0)
       throw StatusError(PALIWA_GB_RUNTIME_ERROR,
-                        "windowed stage planned without a shadow buffer");
-    // Windows overlap their neighbours' segments, so they read the grid and
-    // store to the shadow; a copy stage (a window job without levels and
-    // without halo) then moves the shadow back into the grid.
+                        "windowed stage planned without a halo buffer");
+    // Windows read their halos from the neighbouring segments, which those
+    // segments' windows overwrite in place: a halo pass first copies the
+    // points around every segment boundary to the halo buffer, and the
+    // windows read every point outside their own segment from there.
+    Stage hs;
+    hs.R = kHalo;
+    hs.job = make_job(v, shifts, first, 0);
+    hs.job.dst_base = v.shadow;
+    hs.job.periodic = 0;
+    hs.job.seg_len = static_cast<int>(seg_len);
+    hs.job.halo = static_cast<int>(halo);
+    // Columns per tile: contiguous rows of up to 128 columns on strided
+    // axes; on the last axis about 8192 points per tile.
+    int const log2cols = 63 - __builtin_clzll(static_cast<unsigned long long>(
+                                   v.columns));
+    int lc = 0;
+    if (v.log2_kstride == 0) {
+      while ((2 * halo << (lc + 1)) <= 8192) ++lc;
+    } else {
+      lc = std::max(4, std::min(v.log2_inner, 7));
+    }
+    lc = std::min(lc, log2cols);
+    hs.job.log2_window = lc;
+    hs.job.col_tiles = ceil_div(v.columns, 1LL << lc);
+    long long const nseg = ceil_div(1LL << v.log2_n, seg_len);
+    hs.tiles = nseg * hs.job.col_tiles;
+    out.push_back(hs);
     Stage st;
     st.R = R;
     st.job = make_job(v, shifts, first, count);
-    st.job.dst_base = v.shadow;
+    st.job.halo_base = v.shadow;
     st.job.periodic = 0;
     st.job.log2_window = kWindowLog2;
     st.job.seg_len = static_cast<int>(seg_len);
     st.job.halo = static_cast<int>(halo);
     st.job.col_tiles = ceil_div(v.columns, C);
-    st.tiles = ceil_div(1LL << v.log2_n, seg_len) * st.job.col_tiles;
+    st.tiles = nseg * st.job.col_tiles;
     out.push_back(st);
-    Stage cp;
-    cp.job = make_job(v, shifts, first, 0);
-    cp.job.base = v.shadow;
-    cp.job.dst_base = v.base;
-    long long const bytes = (v.columns << v.log2_n) << v.log2_es;
-    if (v.log2_kstride == v.log2_inner && v.log2_row > 0 &&
-        v.shadow % 16 == 0 && bytes % 16 == 0) {
-      // The whole grid, contiguous in both buffers: a flat copy.
-      cp.R = kCopy;
-      cp.job.columns = bytes;
-      cp.tiles = ceil_div(bytes, kCopyTileBytes);
-    } else {
-      // A sub-lattice, or unaligned buffers: a window pass without levels.
-      cp.R = R;
-      cp.job.periodic = 0;
-      cp.job.log2_window = kWindowLog2;
-      cp.job.seg_len = static_cast<int>(window);
-      cp.job.halo = 0;
-      cp.job.col_tiles = ceil_div(v.columns, C);
-      cp.tiles = ceil_div(1LL << v.log2_n, window) * cp.job.col_tiles;
-    }
-    out.push_back(cp);
     first += count;
   }
 }
@@ -451,7 +449,7 @@ void launch_lift(int dtype, bool exact, bool symmetric, int sched, int R,
   params.njobs = njobs;
   params.total_tiles = total_tiles;
   params.rounds = kRounds;
-  if (R == kCopy) return launch_copy(params, s);
+  if (R == kHalo) return launch_halo(dtype, params, s);
   if (R > kWide) {  // the wide and tile kernels
     switch (dtype) {
     case PALIWA_GB_F64: return launch_wide_f64(sched, R, params, s);
@@ -662,9 +660,20 @@ int paliwa_gb_dehierarchize(void *grid, int dtype, int ndim,
 
 namespace pgb {
 
-void launch_copy(LiftParams const &p, cudaStream_t s) {
-  static thread_local Occupancy occ;
-  launch_persistent(copy_kernel<kThreads>, 0, p, s, occ);
+void launch_halo(int dtype, LiftParams const &p, cudaStream_t s) {
+  if (dtype == PALIWA_GB_F64) {
+    static thread_local Occupancy occ;
+    launch_persistent(halo_kernel<double, kThreads>, 0, p, s, occ);
+  } else {
+    static thread_local Occupancy occ;
+    launch_persistent(halo_kernel<float, kThreads>, 0, p, s, occ);
+  }
+}
+
+long long stage_points(Stage const &st) {
+  if (st.R != kHalo) return st.job.columns << st.job.log2_n;
+  long long const nseg = ceil_div(1LL << st.job.log2_n, st.job.seg_len);
+  return st.job.columns * nseg * 2 * st.job.halo;
 }
 
 } // namespace pgb

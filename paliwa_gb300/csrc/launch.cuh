@@ -24,8 +24,16 @@ struct Occupancy {
   int sms[kMaxDevices] = {};
 };
 
+// CTAs per SM of a persistent launch: as many as fit, capped by `cap` when
+// cap > 0 (fewer CTAs per SM leave room for the launches of other streams
+// to run on the same SMs).
+inline int capped_per_sm(int fit, int cap) {
+  return cap > 0 && cap < fit ? cap : fit;
+}
+
 // One persistent launch on the current device: as many CTAs as fit on it at
-// once, or one per tile when there are fewer tiles.
+// once (capped by p.ctas_per_sm), or one per tile when there are fewer
+// tiles.
 template <typename Kernel>
 void launch_persistent(Kernel kernel, size_t smem, LiftParams const &p,
                        cudaStream_t s, Occupancy &occ) {
@@ -47,7 +55,8 @@ void launch_persistent(Kernel kernel, size_t smem, LiftParams const &p,
     sms = device_sms();
     per_sm = n < 1 ? 1 : n;
   }
-  long long const resident = static_cast<long long>(per_sm) * sms;
+  long long const resident =
+      static_cast<long long>(capped_per_sm(per_sm, p.ctas_per_sm)) * sms;
   long long const blocks = std::min(p.total_tiles, resident);
   kernel<<<static_cast<unsigned>(blocks), kThreads, smem, s>>>(p);
   cuda_check(cudaGetLastError(), "lifting kernel launch");
@@ -146,7 +155,7 @@ void launch_lift_f32(bool exact, int sched, int R, LiftParams const &p,
                      cudaStream_t s);
 void launch_lift_f32c(bool exact_sym, int sched, int R, LiftParams const &p,
                       cudaStream_t s);
-void launch_copy(LiftParams const &p, cudaStream_t s);
+void launch_halo(int dtype, LiftParams const &p, cudaStream_t s);
 void launch_wide_f64(int sched, int code, LiftParams const &p, cudaStream_t s);
 void launch_wide_f32(int sched, int code, LiftParams const &p, cudaStream_t s);
 void launch_wide_f32c(int sched, int code, LiftParams const &p,

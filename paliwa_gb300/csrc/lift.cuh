@@ -21,7 +21,11 @@
 // phases, planned on the host: the fine levels on overlapping windows
 // (segment plus halo, non-periodic; only the segment is stored), and the
 // coarse levels on the strided sub-lattice of the remaining points, which is
-// itself a short periodic pencil.
+// itself a short periodic pencil. A window's halo lies in the neighbouring
+// segments, which their own windows overwrite in place, so a halo pass
+// (halo_kernel) first copies the points within a halo of every segment
+// boundary to a side buffer of the grid's layout, and the windows read their
+// halos from there.
 #pragma once
 
 #include <cstdint>
@@ -39,10 +43,13 @@ constexpr int kMaxLevels = 48;
 // along one axis. Jobs of a launch are sorted by tile_begin.
 struct LiftJob {
   unsigned long long base;  // byte address of the grid's first element
-  // Byte address the results are stored to (same layout). Equal to `base`
-  // for in-place stages; windowed stages store to a shadow buffer, because
-  // their halos overlap the neighbouring windows' stored segments.
+  // Byte address the results are stored to (same layout; `base` for every
+  // stage the planner makes).
   unsigned long long dst_base;
+  // Windows: byte address of a buffer in the grid's layout holding the
+  // points around the segment boundaries, from which the window reads every
+  // point outside its own segment (0: read them from `base`).
+  unsigned long long halo_base;
   long long columns;        // outer * inner
   long long tile_begin;     // index of the first tile of this job
   long long col_tiles;      // tiles per window row (ceil(columns / C))
@@ -66,6 +73,7 @@ struct LiftParams {
   long long total_tiles;
   int npasses;
   int rounds;           // column rounds per tile (tile = rounds * NT * R)
+  int ctas_per_sm;      // cap on a persistent launch's CTAs per SM (0: none)
   unsigned c1_one_mask;
   int offsets[kMaxPasses];
   Coeffs coeffs[kMaxPasses];
@@ -697,19 +705,36 @@ __device__ __forceinline__ void store_chunk(S *p, long long kstride, bool vec,
 //    copied as 16-byte vectors (the last axis);
 //  * scalar: anything else (narrow inner extents, sub-lattices).
 // Stores (Store == true) keep only in-range columns and, for windows, the
-// points k in [halo, halo + seg_len) that fall inside the pencil.
+// points k in [halo, halo + seg_len) that fall inside the pencil. Loads of a
+// window take those points from the grid and every other point from the
+// halo buffer (same offsets).
 template <typename S, int R, int NT> struct TileCopy {
   static constexpr int VEC = 16 / sizeof(S);
   static constexpr int LOG2R = Log2<R>::value;
   LiftJob const &job;
   int periodic, log2W, cols, pitch;
   long long gc0, wstart, n;
-  unsigned char *gbase;
+  unsigned char *gbase, *hbase;
 
   __device__ TileCopy(LiftJob const &j, int per, int lw, int c, long long g0,
                       long long ws, long long nn, int pt, unsigned char *gb)
       : job(j), periodic(per), log2W(lw), cols(c), pitch(pt), gc0(g0),
-        wstart(ws), n(nn), gbase(gb) {}
+        wstart(ws), n(nn), gbase(gb),
+        hbase(j.halo_base ? reinterpret_cast<unsigned char *>(j.halo_base)
+                          : gb) {}
+
+  // Point k of the tile belongs to the window's own segment (always, for a
+  // periodic pencil): it is loaded from the grid, else from the halo buffer.
+  // Segment bounds are multiples of 16 points, so a vector of up to 16
+  // consecutive points along k is either all inside or all outside.
+  __device__ __forceinline__ bool own(int k) const {
+    return periodic || (static_cast<unsigned>(k - job.halo) <
+                            static_cast<unsigned>(job.seg_len) &&
+                        wstart + k < n);
+  }
+  __device__ __forceinline__ S const *source(int k) const {
+    return reinterpret_cast<S const *>(own(k) ? gbase : hbase);
+  }
 
   __device__ __forceinline__ int sidx(int w, int k) const {
     return w * pitch + (k >> LOG2R) * (R + 1) + (k & (R - 1));
@@ -759,14 +784,17 @@ template <typename S, int R, int NT> struct TileCopy {
     if (log2B >= 31 - __clz(cols)) {
       if (q >= room) return;
       int const drho = NT >> log2RL;  // rows per step, a multiple of R
-      int const k0 = t >> log2RL;
-      long long pk = pos(k0);  // pencil position of row k0 + i * drho
-      int sb = sidx(q, k0);
+      int k = t >> log2RL;
+      long long pk = pos(k);  // pencil position of row k
+      int sb = sidx(q, k);
       int const dsb = (drho >> LOG2R) * (R + 1);
       S const *const gq = g + base + q;
+      S const *const hq = reinterpret_cast<S const *>(hbase) + base + q;
 #pragma unroll 8
       for (int i = 0; i < PER; ++i) {
-        cp_async<sizeof(S)>(stage + sb, gq + (pk << job.log2_kstride));
+        cp_async<sizeof(S)>(stage + sb,
+                            (own(k) ? gq : hq) + (pk << job.log2_kstride));
+        k += drho;
         pk += drho;
         if (pk >= n) pk -= n;  // a window wrapping around the period
         sb += dsb;
@@ -784,7 +812,7 @@ template <typename S, int R, int NT> struct TileCopy {
       long long const off =
           base + (static_cast<long long>(a_off) << job.log2_astride) +
           (pos(k) << job.log2_kstride) + q;
-      cp_async<sizeof(S)>(stage + sidx(w, k), g + off);
+      cp_async<sizeof(S)>(stage + sidx(w, k), source(k) + off);
     }
   }
 
@@ -808,10 +836,10 @@ template <typename S, int R, int NT> struct TileCopy {
     long long const a0 = gc0 >> log2B;
     long long const b0 = gc0 & ((1LL << log2B) - 1);
     long long const columns = job.columns;
-    auto locate = [&](int v, long long &off, int &sb) -> bool {
+    auto locate = [&](int v, long long &off, int &sb, int &k) -> bool {
       int const rho = v >> log2vpr;
       int const q = v & ((1 << log2vpr) - 1);
-      int const k = rho & ((1 << log2W) - 1);
+      k = rho & ((1 << log2W) - 1);
       int const a_off = rho >> log2W;
       int const w0 = (a_off << log2RL) + q * VW;
       off = ((a0 + a_off) << job.log2_astride) + b0 +
@@ -822,8 +850,8 @@ template <typename S, int R, int NT> struct TileCopy {
 #pragma unroll 4
     for (int i = 0; i < PER; ++i) {
       long long off;
-      int sb;
-      bool const ok = locate(t + i * NT, off, sb);
+      int sb, k;
+      bool const ok = locate(t + i * NT, off, sb, k);
       if (!ok) continue;
       if constexpr (Store) {
         S tmp[VW];
@@ -835,9 +863,10 @@ template <typename S, int R, int NT> struct TileCopy {
       } else {
         // element-wise asynchronous copies into the padded layout (the
         // elements of one vector land `pitch` apart)
+        S const *const src = source(k) + off;
 #pragma unroll
         for (int e = 0; e < VW; ++e)
-          cp_async<sizeof(S)>(stage + sb + e * pitch, g + off + e);
+          cp_async<sizeof(S)>(stage + sb + e * pitch, src + e);
       }
     }
   }
@@ -873,9 +902,10 @@ template <typename S, int R, int NT> struct TileCopy {
           memcpy(&u, tmp, 16);
           *reinterpret_cast<uint4 *>(g + off) = u;
         } else {
+          S const *const src = source(k) + off;
 #pragma unroll
           for (int e = 0; e < VEC; ++e)
-            cp_async<sizeof(S)>(stage + sb + e, g + off + e);
+            cp_async<sizeof(S)>(stage + sb + e, src + e);
         }
       }
       return;
@@ -1704,17 +1734,20 @@ __global__ void __launch_bounds__(NT, 2)
   cp_async_wait_all();
 }
 
-// Copy kernel: each job moves `columns` bytes (a multiple of 16, both ends
-// 16-byte aligned) from `base` to `dst_base`; a tile is kCopyTileBytes of
-// one job. It returns the windowed stages' shadow buffer to the grid: a
-// flat copy at HBM speed instead of a lifting pass over windows with no
-// levels.
-constexpr int kCopyTileBytes = 1 << 16;
-
-template <int NT>
+// Halo kernel: runs before a windowed stage and copies, from the grid
+// (`base`) to the halo buffer (`dst_base`, same offsets), the points within
+// `halo` of every segment boundary b * seg_len, b = 0 .. ceil(n / seg_len)
+// - 1 (positions [b seg_len - halo, b seg_len + halo) modulo n): every point
+// a window reads outside its own segment, taken before the windows overwrite
+// their segments in place. Boundaries closer than 2 halo (a short last
+// segment) copy some points twice, with the same values. A tile is one
+// boundary of 2^log2_window columns; the points of a tile are visited with
+// the grid's contiguous direction fastest: along the pencil for the last
+// axis, along the columns otherwise.
+template <typename S, int NT>
 __global__ void __launch_bounds__(NT)
-    copy_kernel(__grid_constant__ const LiftParams p) {
-  constexpr int PER = kCopyTileBytes / 16 / NT;  // 16-byte vectors / thread
+    halo_kernel(__grid_constant__ const LiftParams p) {
+  constexpr int UNROLL = 4;
   int const t = threadIdx.x;
   int const lane = t & 31;
   __shared__ JobSlot wjobs[NT / 32];
@@ -1724,20 +1757,45 @@ __global__ void __launch_bounds__(NT)
   cur.init(p, &wjobs[t >> 5], first, lane);
   for (long long tile = first; tile < p.total_tiles; tile += gridDim.x) {
     LiftJob const &job = cur.at(p, tile, lane);
-    long long const off = (tile - job.tile_begin) * kCopyTileBytes;
-    long long const left = job.columns - off;  // bytes left in the job
-    uint4 const *src = reinterpret_cast<uint4 const *>(job.base + off);
-    uint4 *dst = reinterpret_cast<uint4 *>(job.dst_base + off);
-    uint4 v[PER];
+    long long const local = tile - job.tile_begin;
+    long long const bnd = local / job.col_tiles;
+    int const log2C = job.log2_window;
+    long long const gc0 = (local - bnd * job.col_tiles) << log2C;
+    int const span = 2 * job.halo;
+    int const total = span << log2C;
+    long long const n = 1LL << job.log2_n;
+    long long const p0 = bnd * job.seg_len - job.halo;
+    bool const along = job.log2_kstride == 0;
+    long long const imask = (1LL << job.log2_inner) - 1;
+    S const *const src = reinterpret_cast<S const *>(job.base);
+    S *const dst = reinterpret_cast<S *>(job.dst_base);
+    for (int i0 = t; i0 < total; i0 += UNROLL * NT) {
+      long long off[UNROLL];
+      bool ok[UNROLL];
+      S v[UNROLL];
 #pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      long long const b = static_cast<long long>(i * NT + t) * 16;
-      if (b < left) v[i] = src[i * NT + t];
-    }
+      for (int u = 0; u < UNROLL; ++u) {
+        int const i = i0 + u * NT;
+        int w, j;
+        if (along) {
+          w = i / span;
+          j = i - w * span;
+        } else {
+          w = i & ((1 << log2C) - 1);
+          j = i >> log2C;
+        }
+        long long pp = p0 + j;
+        if (pp < 0) pp += n;
+        if (pp >= n) pp -= n;
+        long long const gc = gc0 + w;
+        ok[u] = i < total && gc < job.columns;
+        off[u] = ((gc >> job.log2_inner) << job.log2_astride) + (gc & imask) +
+                 (pp << job.log2_kstride);
+        if (ok[u]) v[u] = src[off[u]];
+      }
 #pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      long long const b = static_cast<long long>(i * NT + t) * 16;
-      if (b < left) dst[i * NT + t] = v[i];
+      for (int u = 0; u < UNROLL; ++u)
+        if (ok[u]) dst[off[u]] = v[u];
     }
   }
 }

@@ -39,8 +39,8 @@ bool symmetric_filters(std::vector<Filter> const &filters);
 // A dense view of the pencils along one axis.
 struct AxisView {
   unsigned long long base = 0;  // byte address of the grid
-  // Byte address of a buffer with the grid's size and layout, used by the
-  // windowed stages of pencils longer than one CTA holds (0: none).
+  // Byte address of a buffer with the grid's size and layout that holds the
+  // windowed stages' halos (pencils longer than one CTA holds; 0: none).
   unsigned long long shadow = 0;
   long long columns = 1;        // outer * inner
   int log2_inner = 0;
@@ -69,8 +69,8 @@ constexpr int kWide = 64;
 constexpr int kWideContig = 128;
 constexpr int kTile = 192;
 constexpr int kTileLong = 256;
-// Stage::R of a flat copy (copy_kernel): job.columns counts bytes.
-constexpr int kCopy = 512;
+// Stage::R of a halo pass (halo_kernel) before a windowed stage.
+constexpr int kHalo = 512;
 
 // One stage of an axis transform: a job for one kernel. The stages of one
 // axis must run in order; stages of different grids are independent.
@@ -79,7 +79,7 @@ struct Stage {
   long long tiles = 0;
   LiftJob job{};
   // Periodic stages: the tuning class and the kernels that apply (a bit per
-  // KernelChoice); 0 for windowed and copy stages.
+  // KernelChoice); 0 for windowed and halo stages.
   int tclass = 0;
   unsigned kernels = 0;
   int dflt = 0;
@@ -117,6 +117,11 @@ int tuning_class(AxisView const &v);
 void plan_axis(AxisView const &view, std::vector<int> const &shifts,
                std::vector<Filter> const &filters, std::vector<Stage> &out,
                Tuning const *tuning = nullptr);
+
+// Points one stage reads and writes (the algorithmic bytes of its launch are
+// twice this times the element size): every point of its pencils, or for a
+// halo pass the points it copies.
+long long stage_points(Stage const &st);
 
 // True when planning `view` along `shifts` needs a shadow buffer.
 inline bool needs_shadow(AxisView const &view, std::vector<int> const &shifts) {

@@ -61,9 +61,11 @@ struct SlabJob {
 struct SlabParams {
   CUtensorMap map;          // [rows][128 bytes] over the batch's grids
   SlabJob const *jobs;      // sorted by tile_begin
+  int const *tile_job;      // the job of every tile of the launch
   int njobs;
   long long total_tiles;
   unsigned *error;          // set to 1 when a bounded wait gives up
+  int ctas_per_sm;          // cap on the launch's CTAs per SM (0: none)
 };
 
 // ---- PTX wrappers (sm_90+ bulk tensor copies and mbarriers)
@@ -273,20 +275,6 @@ __device__ __forceinline__ void slab_axis(unsigned char *tile, SlabAxis ax,
   }
 }
 
-// Last job whose first tile is <= tile.
-__device__ __forceinline__ int slab_find_job(SlabParams const &p,
-                                             long long tile) {
-  int lo = 0, hi = p.njobs - 1;
-  while (lo < hi) {
-    int const mid = (lo + hi + 1) >> 1;
-    if (p.jobs[mid].tile_begin <= tile)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
 // Dynamic shared memory: the tile buffers (1 KB aligned for the swizzle,
 // plus 1 KB of alignment slack) and the chunk heads and exchange buffers.
 template <class A> constexpr size_t slab_smem_bytes() {
@@ -326,17 +314,19 @@ __global__ void __launch_bounds__(kSlabThreads, 2)
   }
   __syncthreads();
 
-  // Warp 0 issues the copies: lane 0 the job lookup and the transaction
-  // count, every lane some of the tile's 1 KB boxes.
-  int ji = 0;  // job cursor of warp 0 (tiles only increase)
+  // Warp 0 issues the copies: the job of the tile (one table lookup, its
+  // words copied by the lanes in parallel), lane 0 the transaction count,
+  // every lane some of the tile's 1 KB boxes.
+  constexpr int kJobWords = sizeof(SlabJob) / 4;
+  static_assert(sizeof(SlabJob) % 4 == 0 && kJobWords <= 32,
+                "a slab job is copied one word per lane");
   auto issue_load = [&](long long k) {
     int const b = static_cast<int>(k % kSlabStages);
     long long const tile = first + k * step;
-    if (lane == 0) {
-      if (ji + 1 < p.njobs && p.jobs[ji + 1].tile_begin <= tile)
-        ji = slab_find_job(p, tile);
-      sjob[b] = p.jobs[ji];
-    }
+    int const j = p.tile_job[tile];
+    if (lane < kJobWords)
+      reinterpret_cast<unsigned *>(&sjob[b])[lane] =
+          reinterpret_cast<unsigned const *>(p.jobs + j)[lane];
     __syncwarp();
     SlabJob const &job = sjob[b];
     int const bytes = 1 << (job.log2_tile + LOG2ES);

@@ -29,7 +29,8 @@ void launch_slab_r(SlabParams const &p, cudaStream_t s) {
     sms = device_sms();
     per_sm = n < 1 ? 1 : n;
   }
-  long long const resident = static_cast<long long>(per_sm) * sms;
+  long long const resident =
+      static_cast<long long>(capped_per_sm(per_sm, p.ctas_per_sm)) * sms;
   long long const blocks = std::min(p.total_tiles, resident);
   kernel<<<static_cast<unsigned>(blocks), kSlabThreads, smem, s>>>(p);
   cuda_check(cudaGetLastError(), "slab kernel launch");

@@ -77,7 +77,7 @@ def kernel_name(code):
     if code == SLAB_KERNEL:
         return "slab_kernel"
     if code == 512:
-        return "copy_kernel"
+        return "halo_kernel"
     if code > 256:
         return f"tile_kernel long R={code - 256}"
     if code > 192:
@@ -145,6 +145,13 @@ class Batch:
         slab launch (default), or every axis on its own (the same bits).
         Synchronizes the device."""
         _lib.check(self._lib.paliwa_gb_batch_use_slabs(self._h, int(enable)))
+
+    def set_ctas_per_sm(self, ctas):
+        """Cap every launch of the batch at ``ctas`` CTAs per SM, leaving
+        room on each SM for the other groups' launches (0: as many as fit,
+        the default). Synchronizes the device."""
+        _lib.check(self._lib.paliwa_gb_batch_set_ctas_per_sm(self._h,
+                                                             int(ctas)))
 
     def status(self):
         """Raises DeviceTimeout if a slab launch gave up a bounded wait for

@@ -340,21 +340,15 @@ void plan_windows(AxisView const &v, std::vector<int> const &shifts,
     hs.job.periodic = 0;
     hs.job.seg_len = static_cast<int>(seg_len);
     hs.job.halo = static_cast<int>(halo);
-    // Columns per tile: contiguous rows of up to 128 columns on strided
-    // axes; on the last axis about 8192 points per tile.
+    // A tile: 32 positions around one boundary of up to 64 columns (2048
+    // points, many tiles in flight for these small passes).
     int const log2cols = 63 - __builtin_clzll(static_cast<unsigned long long>(
                                    v.columns));
-    int lc = 0;
-    if (v.log2_kstride == 0) {
-      while ((2 * halo << (lc + 1)) <= 8192) ++lc;
-    } else {
-      lc = std::max(4, std::min(v.log2_inner, 7));
-    }
-    lc = std::min(lc, log2cols);
+    int const lc = std::min(6, log2cols);
     hs.job.log2_window = lc;
     hs.job.col_tiles = ceil_div(v.columns, 1LL << lc);
     long long const nseg = ceil_div(1LL << v.log2_n, seg_len);
-    hs.tiles = nseg * hs.job.col_tiles;
+    hs.tiles = nseg * (halo / 16) * hs.job.col_tiles;
     out.push_back(hs);
     Stage st;
     st.R = R;

@@ -707,8 +707,9 @@ __device__ __forceinline__ void store_chunk(S *p, long long kstride, bool vec,
 // Stores (Store == true) keep only in-range columns and, for windows, the
 // points k in [halo, halo + seg_len) that fall inside the pencil. Loads of a
 // window take those points from the grid and every other point from the
-// halo buffer (same offsets).
-template <typename S, int R, int NT> struct TileCopy {
+// halo buffer (same offsets). A TileCopy moves ROUNDS column rounds (cols =
+// ROUNDS * NT / G columns, NT * ROUNDS * R points).
+template <typename S, int R, int NT, int ROUNDS = kTileRounds> struct TileCopy {
   static constexpr int VEC = 16 / sizeof(S);
   static constexpr int LOG2R = Log2<R>::value;
   LiftJob const &job;
@@ -773,7 +774,7 @@ template <typename S, int R, int NT> struct TileCopy {
   // advance by constants (for windows, modulo the pencil length).
   __device__ __forceinline__ void rows_load(S *stage, int t,
                                             int log2RL) const {
-    constexpr int PER = kTileRounds * R;  // elements per thread
+    constexpr int PER = ROUNDS * R;  // elements per thread
     S const *const g = reinterpret_cast<S const *>(gbase);
     int const log2B = job.log2_inner;
     long long const base = ((gc0 >> log2B) << job.log2_astride) +
@@ -828,7 +829,7 @@ template <typename S, int R, int NT> struct TileCopy {
         typename std::conditional<VW * sizeof(S) == 8, uint2,
                                   unsigned>::type>::type;
     static_assert(VW * sizeof(S) == sizeof(U), "vector width");
-    constexpr int PER = kTileRounds * R / VW;  // vectors per thread
+    constexpr int PER = ROUNDS * R / VW;  // vectors per thread
     S *const g = reinterpret_cast<S *>(
         Store ? reinterpret_cast<unsigned char *>(job.dst_base) : gbase);
     int const log2B = job.log2_inner;
@@ -883,7 +884,7 @@ template <typename S, int R, int NT> struct TileCopy {
     if (aligned && VEC > 1 && log2B == 0 && job.log2_kstride == 0 &&
         R >= VEC) {
       // each column contiguous along k
-      constexpr int PER = kTileRounds * R / VEC;
+      constexpr int PER = ROUNDS * R / VEC;
       int const log2vpc = log2W - Log2<VEC>::value;
 #pragma unroll 4
       for (int i = 0; i < PER; ++i) {
@@ -969,13 +970,44 @@ __device__ __forceinline__ void fetch_job(LiftParams const &p, long long tile,
   }
 }
 
+// Geometry of one staged tile, from its job: chunks per column, columns per
+// round, the padded pitch of a column in shared memory, the window segment
+// and the tile's first column.
+template <class A, int R, int NT> struct StagedTile {
+  using S = typename A::Store;
+  static constexpr int LOG2R = Log2<R>::value;
+  static constexpr int LOG2NT = Log2<NT>::value;
+  int log2W, log2G, log2CR, pitch, periodic;
+  long long n, seg, gc0, wstart;
+
+  __device__ __forceinline__ StagedTile(LiftJob const &job, long long tile) {
+    log2W = job.log2_window;  // points per column held
+    log2G = log2W - LOG2R;    // chunks per column
+    log2CR = LOG2NT - log2G;  // columns per round
+    static_assert(kTileRounds == 2, "tile_pitch takes log2(cols) = log2CR + 1");
+    pitch = tile_pitch<R, S>(1 << log2G, job.log2_inner, log2CR + 1,
+                             TileCopy<S, R, NT>::contiguous(job));
+    periodic = job.periodic;
+    n = 1LL << job.log2_n;
+    long long const local = tile - job.tile_begin;
+    seg = local / job.col_tiles;
+    gc0 = (local - seg * job.col_tiles) * (kTileRounds << log2CR);
+    wstart = periodic ? 0 : seg * job.seg_len - job.halo;  // window origin
+  }
+  // The copy of round r's columns (shared-memory region r).
+  __device__ __forceinline__ TileCopy<S, R, NT, 1> round(LiftJob const &job,
+                                                         int r) const {
+    return TileCopy<S, R, NT, 1>(
+        job, periodic, log2W, 1 << log2CR,
+        gc0 + (static_cast<long long>(r) << log2CR), wstart, n, pitch,
+        reinterpret_cast<unsigned char *>(job.base));
+  }
+};
+
 // Direct: every job of the launch is a periodic pencil of n == R points held
-// by one thread (no staging); otherwise tiles are staged through shared
-// memory. The two paths are separate instantiations so that neither's
-// register budget constrains the other.
-template <class A, int R, int NT, class Sched, bool Direct>
-__global__ void __launch_bounds__(NT)
-    lift_kernel(__grid_constant__ const LiftParams p) {
+// by one thread (no staging); pencils go straight between HBM and registers.
+template <class A, int R, int NT, class Sched>
+__device__ __forceinline__ void lift_direct(LiftParams const &p) {
   using V = typename A::V;
   using S = typename A::Store;
   constexpr int LOG2R = Log2<R>::value;
@@ -983,7 +1015,6 @@ __global__ void __launch_bounds__(NT)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *heads = reinterpret_cast<V *>(smem_raw);
   V *xch = heads + NT;  // two buffers of NT
-  S *stage = reinterpret_cast<S *>(xch + 2 * NT);
 
   int const t = threadIdx.x;
   int const lane = t & 31;
@@ -995,7 +1026,7 @@ __global__ void __launch_bounds__(NT)
   // Persistent CTAs: tiles are visited in increasing order, so the job
   // cursor only moves forward.
   for (long long tile = blockIdx.x; tile < p.total_tiles; tile += gridDim.x) {
-    __syncthreads();  // the previous tile is out of shared memory
+    __syncthreads();  // every thread is done with the previous job
     fetch_job<NT>(p, tile, t, ji, sjob, sjob_index);
     int const log2W = job->log2_window;       // points per column held
     int const log2G = log2W - LOG2R;          // chunks per column
@@ -1003,22 +1034,12 @@ __global__ void __launch_bounds__(NT)
     int const log2CR = LOG2NT - log2G;        // columns per round
     constexpr int rounds = kTileRounds;
     int const cols = rounds << log2CR;        // columns per tile
-    int const pitch = tile_pitch<R, typename A::Store>(
-        G, job->log2_inner, LOG2NT - log2G + 1,
-        TileCopy<typename A::Store, R, NT>::contiguous(*job));
-    static_assert(kTileRounds == 2, "tile_pitch takes log2(cols) = log2CR + 1");
     int const periodic = job->periodic;
-    long long const n = 1LL << job->log2_n;
-
     long long const local = tile - job->tile_begin;
     long long const seg = local / job->col_tiles;
     long long const gc0 = (local - seg * job->col_tiles) * cols;
-    long long const wstart =
-        periodic ? 0 : seg * job->seg_len - job->halo;  // window origin
-
     unsigned char *const gbase = reinterpret_cast<unsigned char *>(job->base);
-
-    if constexpr (Direct) {
+    {
       // Pencils straight between HBM and registers, no staging and no
       // barrier: either one whole pencil per thread (n == R, lanes along
       // columns), or a contiguous pencil (last axis) of G <= 32 chunks held
@@ -1059,37 +1080,97 @@ __global__ void __launch_bounds__(NT)
                               kstride, vec, raw);
         }
       }
-      continue;
-    } else {
-    (void)G;
-
-    // ---- load: global -> stage
-    TileCopy<S, R, NT> cp(*job, periodic, log2W, cols, gc0, wstart, n, pitch,
-                          gbase);
-    cp.template run<false>(stage, t, seg, 0, 0);
-    cp_async_wait_all();
-    __syncthreads();
-
-    // ---- compute: one round = NT / G columns, thread = (column, chunk)
-    for (int r = 0; r < rounds; ++r) {
-      int const c = t & (G - 1);
-      int const wl = (r << log2CR) + (t >> log2G);
-      S *chunk = stage + wl * pitch + c * (R + 1);
-      V v[R];
-#pragma unroll
-      for (int j = 0; j < R; ++j) v[j] = A::load(chunk[j]);
-      RoundCtx<A, NT> ctx(t, c, G, log2G, lane, periodic, heads, xch);
-      Sched::template run<A, R, NT>(v, ctx, *job, p);
-#pragma unroll
-      for (int j = 0; j < R; ++j) chunk[j] = A::store(v[j]);
-      if (G > 32) __syncthreads();  // heads / xch reused by the next round
-    }
-    __syncthreads();
-
-    // ---- store: stage -> global (only this tile's segment of a window)
-    cp.template run<true>(stage, t, seg, job->halo, job->seg_len);
     }
   }
+}
+
+// Staged: tiles go through shared memory, one region per column round, and
+// the rounds are pipelined across tiles: while a round is transformed, the
+// other region holds (or receives) a round of the same or the next tile, so
+// each CTA keeps one round's loads in flight during its compute. Per round:
+// wait for its copy, transform it in registers, store it, then start the
+// next tile's copy of the same round into the freed region.
+template <class A, int R, int NT, class Sched>
+__device__ __forceinline__ void lift_staged(LiftParams const &p) {
+  using V = typename A::V;
+  using S = typename A::Store;
+  constexpr int HALF = NT * (R + 2);  // elements of one round's region
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *heads = reinterpret_cast<V *>(smem_raw);
+  V *xch = heads + NT;  // two buffers of NT
+  S *stage = reinterpret_cast<S *>(xch + 2 * NT);
+
+  int const t = threadIdx.x;
+  int const lane = t & 31;
+  // Jobs of the current tile and of the next one (alternating slots).
+  __shared__ LiftJob sjob[2];
+  __shared__ int sjob_index[2];
+  long long tile = blockIdx.x;
+  if (tile >= p.total_tiles) return;
+  if (t == 0) sjob_index[0] = sjob_index[1] = -1;
+  __syncthreads();
+  int ji = 0;
+  fetch_job<NT>(p, tile, t, ji, sjob[0], sjob_index[0]);
+  {
+    StagedTile<A, R, NT> const g(sjob[0], tile);
+    for (int r = 0; r < kTileRounds; ++r) {
+      g.round(sjob[0], r).template run<false>(stage + r * HALF, t, g.seg, 0,
+                                              0);
+      cp_async_commit();
+    }
+  }
+  int cur = 0;
+  // Persistent CTAs: tiles are visited in increasing order, so the job
+  // cursor only moves forward.
+  for (; tile < p.total_tiles; tile += gridDim.x) {
+    long long const next = tile + gridDim.x;
+    bool const more = next < p.total_tiles;
+    if (more) fetch_job<NT>(p, next, t, ji, sjob[cur ^ 1], sjob_index[cur ^ 1]);
+    LiftJob const &job = sjob[cur];
+    StagedTile<A, R, NT> const g(job, tile);
+    int const G = 1 << g.log2G;
+    for (int r = 0; r < kTileRounds; ++r) {
+      // Two copy groups are in flight: this round's and the one after it.
+      cp_async_wait_group<1>();
+      __syncthreads();
+      // ---- compute: NT / G columns, thread = (column, chunk)
+      {
+        int const c = t & (G - 1);
+        S *chunk = stage + r * HALF + (t >> g.log2G) * g.pitch + c * (R + 1);
+        V v[R];
+#pragma unroll
+        for (int j = 0; j < R; ++j) v[j] = A::load(chunk[j]);
+        RoundCtx<A, NT> ctx(t, c, G, g.log2G, lane, g.periodic, heads, xch);
+        Sched::template run<A, R, NT>(v, ctx, job, p);
+#pragma unroll
+        for (int j = 0; j < R; ++j) chunk[j] = A::store(v[j]);
+      }
+      __syncthreads();
+      // ---- store: region -> global (only the window's own segment)
+      g.round(job, r).template run<true>(stage + r * HALF, t, g.seg, job.halo,
+                                         job.seg_len);
+      __syncthreads();  // the region is free
+      if (more) {
+        StagedTile<A, R, NT> const gn(sjob[cur ^ 1], next);
+        gn.round(sjob[cur ^ 1], r).template run<false>(stage + r * HALF, t,
+                                                       gn.seg, 0, 0);
+      }
+      cp_async_commit();
+    }
+    cur ^= 1;
+  }
+  cp_async_wait_all();
+}
+
+// The two paths are separate instantiations so that neither's register
+// budget constrains the other.
+template <class A, int R, int NT, class Sched, bool Direct>
+__global__ void __launch_bounds__(NT)
+    lift_kernel(__grid_constant__ const LiftParams p) {
+  if constexpr (Direct)
+    lift_direct<A, R, NT, Sched>(p);
+  else
+    lift_staged<A, R, NT, Sched>(p);
 }
 
 // Wide kernel: each thread holds the same chunk of R points of kCols
@@ -1740,10 +1821,11 @@ __global__ void __launch_bounds__(NT, 2)
 // - 1 (positions [b seg_len - halo, b seg_len + halo) modulo n): every point
 // a window reads outside its own segment, taken before the windows overwrite
 // their segments in place. Boundaries closer than 2 halo (a short last
-// segment) copy some points twice, with the same values. A tile is one
-// boundary of 2^log2_window columns; the points of a tile are visited with
-// the grid's contiguous direction fastest: along the pencil for the last
-// axis, along the columns otherwise.
+// segment) copy some points twice, with the same values. A tile is 32
+// consecutive positions around one boundary (halo is a multiple of 16) of
+// 2^log2_window columns; its points are visited with the grid's contiguous
+// direction fastest: along the pencil for the last axis, along the columns
+// otherwise.
 template <typename S, int NT>
 __global__ void __launch_bounds__(NT)
     halo_kernel(__grid_constant__ const LiftParams p) {
@@ -1758,13 +1840,15 @@ __global__ void __launch_bounds__(NT)
   for (long long tile = first; tile < p.total_tiles; tile += gridDim.x) {
     LiftJob const &job = cur.at(p, tile, lane);
     long long const local = tile - job.tile_begin;
-    long long const bnd = local / job.col_tiles;
+    long long const rest = local / job.col_tiles;
     int const log2C = job.log2_window;
-    long long const gc0 = (local - bnd * job.col_tiles) << log2C;
-    int const span = 2 * job.halo;
-    int const total = span << log2C;
+    long long const gc0 = (local - rest * job.col_tiles) << log2C;
+    int const blocks = job.halo >> 4;  // 32-position blocks per boundary
+    long long const bnd = rest / blocks;
+    int const pb = static_cast<int>(rest - bnd * blocks);
+    int const total = 32 << log2C;
     long long const n = 1LL << job.log2_n;
-    long long const p0 = bnd * job.seg_len - job.halo;
+    long long const p0 = bnd * job.seg_len - job.halo + 32 * pb;
     bool const along = job.log2_kstride == 0;
     long long const imask = (1LL << job.log2_inner) - 1;
     S const *const src = reinterpret_cast<S const *>(job.base);
@@ -1778,8 +1862,8 @@ __global__ void __launch_bounds__(NT)
         int const i = i0 + u * NT;
         int w, j;
         if (along) {
-          w = i / span;
-          j = i - w * span;
+          w = i >> 5;
+          j = i & 31;
         } else {
           w = i & ((1 << log2C) - 1);
           j = i >> log2C;

@@ -707,9 +707,8 @@ __device__ __forceinline__ void store_chunk(S *p, long long kstride, bool vec,
 // Stores (Store == true) keep only in-range columns and, for windows, the
 // points k in [halo, halo + seg_len) that fall inside the pencil. Loads of a
 // window take those points from the grid and every other point from the
-// halo buffer (same offsets). A TileCopy moves ROUNDS column rounds (cols =
-// ROUNDS * NT / G columns, NT * ROUNDS * R points).
-template <typename S, int R, int NT, int ROUNDS = kTileRounds> struct TileCopy {
+// halo buffer (same offsets).
+template <typename S, int R, int NT> struct TileCopy {
   static constexpr int VEC = 16 / sizeof(S);
   static constexpr int LOG2R = Log2<R>::value;
   LiftJob const &job;
@@ -774,7 +773,7 @@ template <typename S, int R, int NT, int ROUNDS = kTileRounds> struct TileCopy {
   // advance by constants (for windows, modulo the pencil length).
   __device__ __forceinline__ void rows_load(S *stage, int t,
                                             int log2RL) const {
-    constexpr int PER = ROUNDS * R;  // elements per thread
+    constexpr int PER = kTileRounds * R;  // elements per thread
     S const *const g = reinterpret_cast<S const *>(gbase);
     int const log2B = job.log2_inner;
     long long const base = ((gc0 >> log2B) << job.log2_astride) +
@@ -829,7 +828,7 @@ template <typename S, int R, int NT, int ROUNDS = kTileRounds> struct TileCopy {
         typename std::conditional<VW * sizeof(S) == 8, uint2,
                                   unsigned>::type>::type;
     static_assert(VW * sizeof(S) == sizeof(U), "vector width");
-    constexpr int PER = ROUNDS * R / VW;  // vectors per thread
+    constexpr int PER = kTileRounds * R / VW;  // vectors per thread
     S *const g = reinterpret_cast<S *>(
         Store ? reinterpret_cast<unsigned char *>(job.dst_base) : gbase);
     int const log2B = job.log2_inner;
@@ -884,7 +883,7 @@ template <typename S, int R, int NT, int ROUNDS = kTileRounds> struct TileCopy {
     if (aligned && VEC > 1 && log2B == 0 && job.log2_kstride == 0 &&
         R >= VEC) {
       // each column contiguous along k
-      constexpr int PER = ROUNDS * R / VEC;
+      constexpr int PER = kTileRounds * R / VEC;
       int const log2vpc = log2W - Log2<VEC>::value;
 #pragma unroll 4
       for (int i = 0; i < PER; ++i) {
@@ -970,44 +969,13 @@ __device__ __forceinline__ void fetch_job(LiftParams const &p, long long tile,
   }
 }
 
-// Geometry of one staged tile, from its job: chunks per column, columns per
-// round, the padded pitch of a column in shared memory, the window segment
-// and the tile's first column.
-template <class A, int R, int NT> struct StagedTile {
-  using S = typename A::Store;
-  static constexpr int LOG2R = Log2<R>::value;
-  static constexpr int LOG2NT = Log2<NT>::value;
-  int log2W, log2G, log2CR, pitch, periodic;
-  long long n, seg, gc0, wstart;
-
-  __device__ __forceinline__ StagedTile(LiftJob const &job, long long tile) {
-    log2W = job.log2_window;  // points per column held
-    log2G = log2W - LOG2R;    // chunks per column
-    log2CR = LOG2NT - log2G;  // columns per round
-    static_assert(kTileRounds == 2, "tile_pitch takes log2(cols) = log2CR + 1");
-    pitch = tile_pitch<R, S>(1 << log2G, job.log2_inner, log2CR + 1,
-                             TileCopy<S, R, NT>::contiguous(job));
-    periodic = job.periodic;
-    n = 1LL << job.log2_n;
-    long long const local = tile - job.tile_begin;
-    seg = local / job.col_tiles;
-    gc0 = (local - seg * job.col_tiles) * (kTileRounds << log2CR);
-    wstart = periodic ? 0 : seg * job.seg_len - job.halo;  // window origin
-  }
-  // The copy of round r's columns (shared-memory region r).
-  __device__ __forceinline__ TileCopy<S, R, NT, 1> round(LiftJob const &job,
-                                                         int r) const {
-    return TileCopy<S, R, NT, 1>(
-        job, periodic, log2W, 1 << log2CR,
-        gc0 + (static_cast<long long>(r) << log2CR), wstart, n, pitch,
-        reinterpret_cast<unsigned char *>(job.base));
-  }
-};
-
 // Direct: every job of the launch is a periodic pencil of n == R points held
-// by one thread (no staging); pencils go straight between HBM and registers.
-template <class A, int R, int NT, class Sched>
-__device__ __forceinline__ void lift_direct(LiftParams const &p) {
+// by one thread (no staging); otherwise tiles are staged through shared
+// memory. The two paths are separate instantiations so that neither's
+// register budget constrains the other.
+template <class A, int R, int NT, class Sched, bool Direct>
+__global__ void __launch_bounds__(NT)
+    lift_kernel(__grid_constant__ const LiftParams p) {
   using V = typename A::V;
   using S = typename A::Store;
   constexpr int LOG2R = Log2<R>::value;
@@ -1015,6 +983,7 @@ __device__ __forceinline__ void lift_direct(LiftParams const &p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *heads = reinterpret_cast<V *>(smem_raw);
   V *xch = heads + NT;  // two buffers of NT
+  S *stage = reinterpret_cast<S *>(xch + 2 * NT);
 
   int const t = threadIdx.x;
   int const lane = t & 31;
@@ -1026,7 +995,7 @@ __device__ __forceinline__ void lift_direct(LiftParams const &p) {
   // Persistent CTAs: tiles are visited in increasing order, so the job
   // cursor only moves forward.
   for (long long tile = blockIdx.x; tile < p.total_tiles; tile += gridDim.x) {
-    __syncthreads();  // every thread is done with the previous job
+    __syncthreads();  // the previous tile is out of shared memory
     fetch_job<NT>(p, tile, t, ji, sjob, sjob_index);
     int const log2W = job->log2_window;       // points per column held
     int const log2G = log2W - LOG2R;          // chunks per column
@@ -1034,12 +1003,22 @@ __device__ __forceinline__ void lift_direct(LiftParams const &p) {
     int const log2CR = LOG2NT - log2G;        // columns per round
     constexpr int rounds = kTileRounds;
     int const cols = rounds << log2CR;        // columns per tile
+    int const pitch = tile_pitch<R, typename A::Store>(
+        G, job->log2_inner, LOG2NT - log2G + 1,
+        TileCopy<typename A::Store, R, NT>::contiguous(*job));
+    static_assert(kTileRounds == 2, "tile_pitch takes log2(cols) = log2CR + 1");
     int const periodic = job->periodic;
+    long long const n = 1LL << job->log2_n;
+
     long long const local = tile - job->tile_begin;
     long long const seg = local / job->col_tiles;
     long long const gc0 = (local - seg * job->col_tiles) * cols;
+    long long const wstart =
+        periodic ? 0 : seg * job->seg_len - job->halo;  // window origin
+
     unsigned char *const gbase = reinterpret_cast<unsigned char *>(job->base);
-    {
+
+    if constexpr (Direct) {
       // Pencils straight between HBM and registers, no staging and no
       // barrier: either one whole pencil per thread (n == R, lanes along
       // columns), or a contiguous pencil (last axis) of G <= 32 chunks held
@@ -1080,97 +1059,37 @@ __device__ __forceinline__ void lift_direct(LiftParams const &p) {
                               kstride, vec, raw);
         }
       }
-    }
-  }
-}
+      continue;
+    } else {
+    (void)G;
 
-// Staged: tiles go through shared memory, one region per column round, and
-// the rounds are pipelined across tiles: while a round is transformed, the
-// other region holds (or receives) a round of the same or the next tile, so
-// each CTA keeps one round's loads in flight during its compute. Per round:
-// wait for its copy, transform it in registers, store it, then start the
-// next tile's copy of the same round into the freed region.
-template <class A, int R, int NT, class Sched>
-__device__ __forceinline__ void lift_staged(LiftParams const &p) {
-  using V = typename A::V;
-  using S = typename A::Store;
-  constexpr int HALF = NT * (R + 2);  // elements of one round's region
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  V *heads = reinterpret_cast<V *>(smem_raw);
-  V *xch = heads + NT;  // two buffers of NT
-  S *stage = reinterpret_cast<S *>(xch + 2 * NT);
+    // ---- load: global -> stage
+    TileCopy<S, R, NT> cp(*job, periodic, log2W, cols, gc0, wstart, n, pitch,
+                          gbase);
+    cp.template run<false>(stage, t, seg, 0, 0);
+    cp_async_wait_all();
+    __syncthreads();
 
-  int const t = threadIdx.x;
-  int const lane = t & 31;
-  // Jobs of the current tile and of the next one (alternating slots).
-  __shared__ LiftJob sjob[2];
-  __shared__ int sjob_index[2];
-  long long tile = blockIdx.x;
-  if (tile >= p.total_tiles) return;
-  if (t == 0) sjob_index[0] = sjob_index[1] = -1;
-  __syncthreads();
-  int ji = 0;
-  fetch_job<NT>(p, tile, t, ji, sjob[0], sjob_index[0]);
-  {
-    StagedTile<A, R, NT> const g(sjob[0], tile);
-    for (int r = 0; r < kTileRounds; ++r) {
-      g.round(sjob[0], r).template run<false>(stage + r * HALF, t, g.seg, 0,
-                                              0);
-      cp_async_commit();
-    }
-  }
-  int cur = 0;
-  // Persistent CTAs: tiles are visited in increasing order, so the job
-  // cursor only moves forward.
-  for (; tile < p.total_tiles; tile += gridDim.x) {
-    long long const next = tile + gridDim.x;
-    bool const more = next < p.total_tiles;
-    if (more) fetch_job<NT>(p, next, t, ji, sjob[cur ^ 1], sjob_index[cur ^ 1]);
-    LiftJob const &job = sjob[cur];
-    StagedTile<A, R, NT> const g(job, tile);
-    int const G = 1 << g.log2G;
-    for (int r = 0; r < kTileRounds; ++r) {
-      // Two copy groups are in flight: this round's and the one after it.
-      cp_async_wait_group<1>();
-      __syncthreads();
-      // ---- compute: NT / G columns, thread = (column, chunk)
-      {
-        int const c = t & (G - 1);
-        S *chunk = stage + r * HALF + (t >> g.log2G) * g.pitch + c * (R + 1);
-        V v[R];
+    // ---- compute: one round = NT / G columns, thread = (column, chunk)
+    for (int r = 0; r < rounds; ++r) {
+      int const c = t & (G - 1);
+      int const wl = (r << log2CR) + (t >> log2G);
+      S *chunk = stage + wl * pitch + c * (R + 1);
+      V v[R];
 #pragma unroll
-        for (int j = 0; j < R; ++j) v[j] = A::load(chunk[j]);
-        RoundCtx<A, NT> ctx(t, c, G, g.log2G, lane, g.periodic, heads, xch);
-        Sched::template run<A, R, NT>(v, ctx, job, p);
+      for (int j = 0; j < R; ++j) v[j] = A::load(chunk[j]);
+      RoundCtx<A, NT> ctx(t, c, G, log2G, lane, periodic, heads, xch);
+      Sched::template run<A, R, NT>(v, ctx, *job, p);
 #pragma unroll
-        for (int j = 0; j < R; ++j) chunk[j] = A::store(v[j]);
-      }
-      __syncthreads();
-      // ---- store: region -> global (only the window's own segment)
-      g.round(job, r).template run<true>(stage + r * HALF, t, g.seg, job.halo,
-                                         job.seg_len);
-      __syncthreads();  // the region is free
-      if (more) {
-        StagedTile<A, R, NT> const gn(sjob[cur ^ 1], next);
-        gn.round(sjob[cur ^ 1], r).template run<false>(stage + r * HALF, t,
-                                                       gn.seg, 0, 0);
-      }
-      cp_async_commit();
+      for (int j = 0; j < R; ++j) chunk[j] = A::store(v[j]);
+      if (G > 32) __syncthreads();  // heads / xch reused by the next round
     }
-    cur ^= 1;
-  }
-  cp_async_wait_all();
-}
+    __syncthreads();
 
-// The two paths are separate instantiations so that neither's register
-// budget constrains the other.
-template <class A, int R, int NT, class Sched, bool Direct>
-__global__ void __launch_bounds__(NT)
-    lift_kernel(__grid_constant__ const LiftParams p) {
-  if constexpr (Direct)
-    lift_direct<A, R, NT, Sched>(p);
-  else
-    lift_staged<A, R, NT, Sched>(p);
+    // ---- store: stage -> global (only this tile's segment of a window)
+    cp.template run<true>(stage, t, seg, job->halo, job->seg_len);
+    }
+  }
 }
 
 // Wide kernel: each thread holds the same chunk of R points of kCols

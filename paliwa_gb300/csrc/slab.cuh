@@ -204,12 +204,15 @@ template <class A, int NT> struct SlabCtx {
   }
 };
 
-// One axis of a tile held in shared memory: every pencil, every level.
-template <class A, int R, int NT, class Sched>
-__device__ __forceinline__ void slab_axis(unsigned char *tile, SlabAxis ax,
-                                          int log2T, int t, int lane,
-                                          typename A::V *heads,
-                                          typename A::V *xch) {
+// U items per thread and iteration of one axis of a tile (U > 1 only for
+// axes whose chunks exchange by shuffle or not at all): the U chunks are
+// independent, so their level steps interleave and hide each other's
+// latencies (short pencils have few updates per chunk).
+template <class A, int R, int NT, class Sched, int U>
+__device__ __forceinline__ void slab_items(unsigned char *tile, SlabAxis ax,
+                                           int log2T, int t, int lane,
+                                           typename A::V *heads,
+                                           typename A::V *xch, bool in_warp) {
   using V = typename A::V;
   using S = typename A::Store;
   constexpr int ES = sizeof(S);
@@ -217,62 +220,97 @@ __device__ __forceinline__ void slab_axis(unsigned char *tile, SlabAxis ax,
   int const log2n = ax.log2n, log2s = ax.log2s;
   int const log2G = log2n - LOG2R;
   int const items = 1 << (log2T - LOG2R);
-  bool const in_warp = log2G + log2s <= 5;
-  for (int base = 0; base < items; base += NT) {
-    int const i = base + t;
-    bool const active = i < items;
-    int const w = i & ((1 << log2s) - 1);
-    int const c = (i >> log2s) & ((1 << log2G) - 1);
-    int const o = i >> (log2s + log2G);
-    // element index of the chunk's first point
-    int const e0 = (o << (log2n + log2s)) + (c << (LOG2R + log2s)) + w;
-    V v[R];
-    if (active) {
-      if (log2s == 0 && R * ES >= 16) {
-        // a contiguous chunk: whole 16-byte pieces
-        constexpr int PER = 16 / ES;
+  bool const vec = log2s == 0 && R * ES >= 16;  // contiguous 16-byte pieces
+  for (int base = 0; base < items; base += U * NT) {
+    int e0[U], c[U];
+    bool active[U];
+    V v[U][R];
 #pragma unroll
-        for (int q = 0; q < R / PER; ++q) {
-          uint4 const u = *reinterpret_cast<uint4 const *>(
-              tile + swz128(e0 * ES + q * 16));
-          S tmp[PER];
-          memcpy(tmp, &u, 16);
+    for (int u = 0; u < U; ++u) {
+      int const i = base + u * NT + t;
+      active[u] = i < items;
+      int const w = i & ((1 << log2s) - 1);
+      c[u] = (i >> log2s) & ((1 << log2G) - 1);
+      int const o = i >> (log2s + log2G);
+      // element index of the chunk's first point
+      e0[u] = (o << (log2n + log2s)) + (c[u] << (LOG2R + log2s)) + w;
+      if (active[u]) {
+        if (vec) {
+          constexpr int PER = 16 / ES;
 #pragma unroll
-          for (int e = 0; e < PER; ++e) v[q * PER + e] = A::load(tmp[e]);
+          for (int q = 0; q < R / PER; ++q) {
+            uint4 const x = *reinterpret_cast<uint4 const *>(
+                tile + swz128(e0[u] * ES + q * 16));
+            S tmp[PER];
+            memcpy(tmp, &x, 16);
+#pragma unroll
+            for (int e = 0; e < PER; ++e) v[u][q * PER + e] = A::load(tmp[e]);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < R; ++j)
+            v[u][j] = A::load(*reinterpret_cast<S const *>(
+                tile + swz128((e0[u] + (j << log2s)) * ES)));
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < R; ++j)
-          v[j] = A::load(*reinterpret_cast<S const *>(
-              tile + swz128((e0 + (j << log2s)) * ES)));
+        for (int j = 0; j < R; ++j) v[u][j] = A::load(S(0));
       }
-    } else {
-#pragma unroll
-      for (int j = 0; j < R; ++j) v[j] = A::load(S(0));
     }
-    SlabCtx<A, NT> ctx(t, c, log2G, lane, log2s, in_warp, heads, xch);
-    Sched::template run_levels<A, R, NT>(v, ctx, ax.nlevels);
-    if (active) {
-      if (log2s == 0 && R * ES >= 16) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      SlabCtx<A, NT> ctx(t, c[u], log2G, lane, log2s, in_warp, heads, xch);
+      Sched::template run_levels<A, R, NT>(v[u], ctx, ax.nlevels);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!active[u]) continue;
+      if (vec) {
         constexpr int PER = 16 / ES;
 #pragma unroll
         for (int q = 0; q < R / PER; ++q) {
           S tmp[PER];
 #pragma unroll
-          for (int e = 0; e < PER; ++e) tmp[e] = A::store(v[q * PER + e]);
-          uint4 u;
-          memcpy(&u, tmp, 16);
-          *reinterpret_cast<uint4 *>(tile + swz128(e0 * ES + q * 16)) = u;
+          for (int e = 0; e < PER; ++e) tmp[e] = A::store(v[u][q * PER + e]);
+          uint4 x;
+          memcpy(&x, tmp, 16);
+          *reinterpret_cast<uint4 *>(tile + swz128(e0[u] * ES + q * 16)) = x;
         }
       } else {
 #pragma unroll
         for (int j = 0; j < R; ++j)
-          *reinterpret_cast<S *>(tile + swz128((e0 + (j << log2s)) * ES)) =
-              A::store(v[j]);
+          *reinterpret_cast<S *>(tile + swz128((e0[u] + (j << log2s)) * ES)) =
+              A::store(v[u][j]);
       }
     }
     if (!in_warp) __syncthreads();  // heads / xch are reused
   }
+}
+
+// One axis of a tile held in shared memory: every pencil, every level.
+// Chunks of up to 8 points run 2 or 4 per thread at once where the axis has
+// enough of them.
+template <class A, int R, int NT, class Sched>
+__device__ __forceinline__ void slab_axis(unsigned char *tile, SlabAxis ax,
+                                          int log2T, int t, int lane,
+                                          typename A::V *heads,
+                                          typename A::V *xch) {
+  constexpr int LOG2R = Log2<R>::value;
+  constexpr int UMAX = R <= 4 ? 4 : (R <= 8 ? 2 : 1);
+  int const log2G = ax.log2n - LOG2R;
+  int const items = 1 << (log2T - LOG2R);
+  // A pencil held by one thread (G == 1) exchanges nothing; otherwise its
+  // chunks are lanes of one warp when G s <= 32.
+  bool const in_warp = log2G == 0 || log2G + ax.log2s <= 5;
+  if constexpr (UMAX > 1) {
+    if (in_warp && items >= UMAX * NT) {
+      slab_items<A, R, NT, Sched, UMAX>(tile, ax, log2T, t, lane, heads, xch,
+                                        true);
+      return;
+    }
+  }
+  slab_items<A, R, NT, Sched, 1>(tile, ax, log2T, t, lane, heads, xch,
+                                 in_warp);
 }
 
 // Dynamic shared memory: the tile buffers (1 KB aligned for the swizzle,

@@ -289,10 +289,10 @@ int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
  * axes planned one by one (when paliwa_gb_batch_use_slabs allows slabs;
  * either way round, the faster kept), then each class of periodic stages
  * (last axis or strided, sub-lattice or not, pencil length, inner extent)
- * and each
- * kernel that applies to it (staged, direct, wide, tile), re-plans and times
- * the whole direction (best of `reps` event-timed runs without a graph) and
- * keeps the fastest choice; classes are tried one after another (coordinate
+ * and each kernel that applies to it (staged, direct, wide, tile),
+ * re-plans and times the whole direction (best of `reps` event-timed runs,
+ * executed as the batch executes it: its groups on parallel branches, from
+ * a graph when graphs are on) and keeps the fastest choice; classes are tried one after another (coordinate
  * descent from the planner's defaults; classes holding under 2 % of the
  * points are left at the default). Runs the transforms on the batch's
  * grids: every timed direction is paired with its inverse, so the contents

@@ -898,17 +898,17 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
 namespace {
 
 // Milliseconds of direction `which` (0 forward, 1 inverse), best of `reps`
-// event-timed runs without a graph; every run is followed (forward) or
-// preceded (inverse) by the other direction, so that the grids return to
-// their contents up to rounding.
+// event-timed runs as the batch runs them (its groups on parallel branches,
+// from a graph when graphs are on: a plan's speed depends on how its
+// launches overlap); every run is followed (forward) or preceded (inverse)
+// by the other direction, so that the grids return to their contents up to
+// rounding.
 float time_direction(paliwa_gb_batch &b, int which, int reps,
                      cudaStream_t s) {
   cudaEvent_t e0, e1;
   cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
   cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
-  auto run = [&](Direction &dr) {
-    for (auto const &L : dr.launches) launch_one(b, dr, L, s);
-  };
+  auto run = [&](Direction &dr) { run_direction(b, dr, s); };
   float best = 1e30f;
   for (int r = 0; r < reps; ++r) {
     if (which == 1) run(b.dir[0]);

@@ -290,6 +290,7 @@ template <class A, int NT> struct RoundCtx {
 // Schedule for arbitrary level lists and filters (transform_in): levels,
 // parities and coefficients are read per step.
 struct RuntimeSched {
+  static constexpr bool kSplit = false;  // no fine_only / coarse_only
   template <class A, int R, int NT, class Ctx>
   static __device__ __forceinline__ void run(typename A::V (&v)[R],
                                              Ctx &ctx,
@@ -362,6 +363,8 @@ template <> struct WaveletPasses<2, false> {
 // The job's shifts are 0 .. L-1 (FWD) or L-1 .. 0.
 template <int W, bool FWD> struct WaveletSched {
   using Passes = typename WaveletPasses<W, FWD>::type;
+  static constexpr bool kForward = FWD;
+  static constexpr bool kSplit = true;  // fine_only / coarse_only below
 
   template <class A, int R, int NT, int K, class P, class Ctx>
   static __device__ __forceinline__ void fine_pass(typename A::V (&v)[R],
@@ -581,6 +584,58 @@ template <int W, bool FWD> struct WaveletSched {
                                              LiftJob const &job,
                                              LiftParams const &) {
     run_levels<A, R, NT>(v, ctx, job.nlevels);
+  }
+
+  // The fine levels (shifts below log2 R) of run_levels alone, the same
+  // operations in the same order; with coarse_only on the chunk heads after
+  // (forward) or before (inverse) them, they make up run_levels.
+  template <class A, int R, int NT, class Ctx>
+  static __device__ __forceinline__ void fine_only(typename A::V (&v)[R],
+                                                   Ctx &ctx, int L) {
+    constexpr int LOG2R = Log2<R>::value;
+    if constexpr (A::kPacked && R >= 4) {
+      constexpr int H = R / 2;
+      DF2 q[H];
+#pragma unroll
+      for (int x = 0; x < H; ++x) {
+        q[x].h = f2_pack(v[x].h, v[x + H].h);
+        q[x].l = f2_pack(v[x].l, v[x + H].l);
+      }
+      if constexpr (FWD)
+        fine_up_packed<A, R, NT, 0>(q, ctx, L);
+      else
+        fine_down_packed<A, R, NT, LOG2R - 1>(q, ctx, L);
+#pragma unroll
+      for (int x = 0; x < H; ++x) {
+        v[x] = {f2_x(q[x].h), f2_x(q[x].l)};
+        v[x + H] = {f2_y(q[x].h), f2_y(q[x].l)};
+      }
+    } else {
+      if constexpr (FWD)
+        fine_up<A, R, NT, 0>(v, ctx, L);
+      else
+        fine_down<A, R, NT, LOG2R - 1>(v, ctx, L);
+    }
+  }
+  // The coarse levels (shifts log2 R .. L-1) of run_levels alone, on the
+  // chunk head `head` of chunks of R points (A may hold the heads of several
+  // columns, e.g. a row policy with one column per lane of a pair).
+  template <class A, int R, int NT, class Ctx>
+  static __device__ __forceinline__ void coarse_only(typename A::V &head,
+                                                     Ctx &ctx, int L) {
+    constexpr int LOG2R = Log2<R>::value;
+    if (L <= LOG2R) return;
+    typename A::V h1[1] = {head};
+    if (!coarse_heads<A, R, NT>(h1[0], ctx, L - LOG2R)) {
+      if constexpr (FWD) {
+        for (int sh = LOG2R; sh < L; ++sh)
+          coarse_level<A, 1, NT>(h1, ctx, 1 << (sh - LOG2R), Passes{});
+      } else {
+        for (int sh = L - 1; sh >= LOG2R; --sh)
+          coarse_level<A, 1, NT>(h1, ctx, 1 << (sh - LOG2R), Passes{});
+      }
+    }
+    head = h1[0];
   }
 
   // The L levels of a job (shifts 0 .. L-1 forward, L-1 .. 0 inverse).
@@ -969,6 +1024,75 @@ __device__ __forceinline__ void fetch_job(LiftParams const &p, long long tile,
   }
 }
 
+// The two column rounds of a staged tile with their coarse levels run
+// together: FP32-compensated chunks under a wavelet schedule whose pencils
+// have coarse levels (more than R points). The fine levels run round by
+// round as before; the two rounds' chunk heads (columns w and w + NT / G,
+// both held by this thread) then form one pair of a row policy of two
+// columns, so each coarse step updates both heads with one set of f32x2
+// operations (the same operations per column: the results are the same
+// bits) and the coarse steps' latency chains are shared by two columns.
+// Forward runs fine levels, then the coarse levels on the heads; inverse
+// the reverse. During the coarse levels the exchange buffer holds the
+// pairs. Returns false (nothing done) when the tile does not qualify.
+template <class A, int R, int NT, class Sched>
+__device__ __forceinline__ bool staged_split_rounds(
+    typename A::Store *stage, int pitch, int G, int log2G, int log2CR, int t,
+    int lane, int periodic, typename A::V *heads, typename A::V *xch,
+    LiftJob const &job) {
+  constexpr int LOG2R = Log2<R>::value;
+  if constexpr (!Sched::kSplit || !std::is_same<A, CompensatedT<true>>::value ||
+                kTileRounds != 2) {
+    return false;
+  } else {
+    using V = typename A::V;
+    using S = typename A::Store;
+    using AR = RowF32C;
+    int const L = job.nlevels;
+    if (L <= LOG2R) return false;
+    int const c = t & (G - 1);
+    S *chunk[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+      chunk[r] = stage + ((r << log2CR) + (t >> log2G)) * pitch + c * (R + 1);
+    V head[2];
+    AR::V *const pairs = reinterpret_cast<AR::V *>(xch);  // NT pairs
+    auto coarse = [&] {
+      AR::V hp = {f2_pack(head[0].h, head[1].h), f2_pack(head[0].l, head[1].l)};
+      RoundCtx<AR, NT> ctx2(t, c, G, log2G, lane, periodic,
+                            reinterpret_cast<AR::V *>(pairs), nullptr);
+      Sched::template coarse_only<AR, R, NT>(hp, ctx2, L);
+      head[0] = {f2_x(hp.h), f2_x(hp.l)};
+      head[1] = {f2_y(hp.h), f2_y(hp.l)};
+    };
+    if constexpr (!Sched::kForward) {
+#pragma unroll
+      for (int r = 0; r < 2; ++r) head[r] = A::load(chunk[r][0]);
+      coarse();
+      if (G > 32) __syncthreads();  // the pairs are out of xch
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      V v[R];
+#pragma unroll
+      for (int j = 0; j < R; ++j) v[j] = A::load(chunk[r][j]);
+      if constexpr (!Sched::kForward) v[0] = head[r];
+      RoundCtx<A, NT> ctx(t, c, G, log2G, lane, periodic, heads, xch);
+      Sched::template fine_only<A, R, NT>(v, ctx, L);
+      if constexpr (Sched::kForward) head[r] = v[0];
+#pragma unroll
+      for (int j = 0; j < R; ++j) chunk[r][j] = A::store(v[j]);
+      if (G > 32) __syncthreads();  // heads / xch reused next
+    }
+    if constexpr (Sched::kForward) {
+      coarse();
+#pragma unroll
+      for (int r = 0; r < 2; ++r) chunk[r][0] = A::store(head[r]);
+    }
+    return true;
+  }
+}
+
 // Direct: every job of the launch is a periodic pencil of n == R points held
 // by one thread (no staging); otherwise tiles are staged through shared
 // memory. The two paths are separate instantiations so that neither's
@@ -1071,18 +1195,22 @@ __global__ void __launch_bounds__(NT)
     __syncthreads();
 
     // ---- compute: one round = NT / G columns, thread = (column, chunk)
-    for (int r = 0; r < rounds; ++r) {
-      int const c = t & (G - 1);
-      int const wl = (r << log2CR) + (t >> log2G);
-      S *chunk = stage + wl * pitch + c * (R + 1);
-      V v[R];
+    if (!staged_split_rounds<A, R, NT, Sched>(stage, pitch, G, log2G, log2CR,
+                                              t, lane, periodic, heads, xch,
+                                              *job)) {
+      for (int r = 0; r < rounds; ++r) {
+        int const c = t & (G - 1);
+        int const wl = (r << log2CR) + (t >> log2G);
+        S *chunk = stage + wl * pitch + c * (R + 1);
+        V v[R];
 #pragma unroll
-      for (int j = 0; j < R; ++j) v[j] = A::load(chunk[j]);
-      RoundCtx<A, NT> ctx(t, c, G, log2G, lane, periodic, heads, xch);
-      Sched::template run<A, R, NT>(v, ctx, *job, p);
+        for (int j = 0; j < R; ++j) v[j] = A::load(chunk[j]);
+        RoundCtx<A, NT> ctx(t, c, G, log2G, lane, periodic, heads, xch);
+        Sched::template run<A, R, NT>(v, ctx, *job, p);
 #pragma unroll
-      for (int j = 0; j < R; ++j) chunk[j] = A::store(v[j]);
-      if (G > 32) __syncthreads();  // heads / xch reused by the next round
+        for (int j = 0; j < R; ++j) chunk[j] = A::store(v[j]);
+        if (G > 32) __syncthreads();  // heads / xch reused by the next round
+      }
     }
     __syncthreads();
 

@@ -1097,8 +1097,11 @@ __device__ __forceinline__ bool staged_split_rounds(
 // by one thread (no staging); otherwise tiles are staged through shared
 // memory. The two paths are separate instantiations so that neither's
 // register budget constrains the other.
+// The staged kernel with 16-point chunks of float grids is held to three
+// CTAs per SM (80 registers).
 template <class A, int R, int NT, class Sched, bool Direct>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(
+    NT, (!Direct && R == 16 && sizeof(typename A::Store) == 4) ? 3 : 1)
     lift_kernel(__grid_constant__ const LiftParams p) {
   using V = typename A::V;
   using S = typename A::Store;

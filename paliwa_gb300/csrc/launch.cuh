@@ -67,8 +67,12 @@ void launch_r(LiftParams const &p, cudaStream_t s) {
   // Direct kernels keep pencils in registers and need no staging memory.
   size_t const smem = Direct ? 0 : lift_smem_bytes<A, R, kThreads>(kRounds);
   static thread_local Occupancy occ;
-  launch_persistent(lift_kernel<A, R, kThreads, Sched, Direct>, smem, p, s,
-                    occ);
+  if constexpr (lift_three_ctas<A, R, Direct>())
+    launch_persistent(lift_kernel3<A, R, kThreads, Sched, Direct>, smem, p, s,
+                      occ);
+  else
+    launch_persistent(lift_kernel<A, R, kThreads, Sched, Direct>, smem, p, s,
+                      occ);
 }
 
 template <class A, int R, class Sched, bool Contig>

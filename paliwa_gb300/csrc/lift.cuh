@@ -1097,12 +1097,8 @@ __device__ __forceinline__ bool staged_split_rounds(
 // by one thread (no staging); otherwise tiles are staged through shared
 // memory. The two paths are separate instantiations so that neither's
 // register budget constrains the other.
-// The staged kernel with 16-point chunks of float grids is held to three
-// CTAs per SM (80 registers).
 template <class A, int R, int NT, class Sched, bool Direct>
-__global__ void __launch_bounds__(
-    NT, (!Direct && R == 16 && sizeof(typename A::Store) == 4) ? 3 : 1)
-    lift_kernel(__grid_constant__ const LiftParams p) {
+__device__ __forceinline__ void lift_body(LiftParams const &p) {
   using V = typename A::V;
   using S = typename A::Store;
   constexpr int LOG2R = Log2<R>::value;
@@ -1221,6 +1217,25 @@ __global__ void __launch_bounds__(
     cp.template run<true>(stage, t, seg, job->halo, job->seg_len);
     }
   }
+}
+
+// The kernel entry points: the register budget is the compiler's for
+// 256-thread CTAs, except for the staged kernel with 16-point chunks of float
+// grids, which is held to three CTAs per SM (80 registers; launch code picks
+// lift_kernel3 for it).
+template <class A, int R, int NT, class Sched, bool Direct>
+__global__ void __launch_bounds__(NT)
+    lift_kernel(__grid_constant__ const LiftParams p) {
+  lift_body<A, R, NT, Sched, Direct>(p);
+}
+template <class A, int R, int NT, class Sched, bool Direct>
+__global__ void __launch_bounds__(NT, 3)
+    lift_kernel3(__grid_constant__ const LiftParams p) {
+  lift_body<A, R, NT, Sched, Direct>(p);
+}
+template <class A, int R, bool Direct>
+constexpr bool lift_three_ctas() {
+  return !Direct && R == 16 && sizeof(typename A::Store) == 4;
 }
 
 // Wide kernel: each thread holds the same chunk of R points of kCols

@@ -393,7 +393,7 @@ def test_batch_groups_give_identical_results(groups):
     joined into the caller's stream, captured into one graph); every group
     count gives the oracle's values bit for bit, through a graph on a
     non-default stream and through direct launches on the legacy stream,
-    including long pencils with shadow-buffer stages in every group."""
+    including long pencils with halo passes in every group."""
     import torch
     levels = [(14, 2), (2, 14), (13, 3), (3, 13), (8, 8), (9, 7), (7, 9),
               (12, 4), (4, 12), (6, 6), (5, 5), (1, 1)]
@@ -416,4 +416,30 @@ def test_batch_groups_give_identical_results(groups):
     torch.cuda.synchronize()
     for g, x in zip(gs, xs):
         assert np.max(np.abs(g.cpu().numpy().reshape(x.shape) - x)) <= 1e-13
+    b.close()
+
+
+@pytest.mark.parametrize("ctas", [1, 3])
+def test_ctas_per_sm_cap_gives_identical_results(ctas):
+    """A cap on the CTAs per SM of every launch changes only how many CTAs
+    walk the tiles: FP64 results equal the oracle's bit for bit, long
+    pencils (halo passes and windows) and slab launches included."""
+    import torch
+    levels = [(14, 2), (2, 14), (13, 3), (8, 8), (6, 6), (5, 5), (3, 4)]
+    lmin, lmax = (1, 1), (14, 14)
+    rng = np.random.default_rng(40 + ctas)
+    xs = [rng.uniform(-1, 1, [1 << l for l in lv]) for lv in levels]
+    buf, gs = pct.packed_grids(levels, torch.float64)
+    for g, x in zip(gs, xs):
+        g.copy_(torch.from_numpy(x).reshape(-1))
+    b = pct.Batch(gs, levels, lmin, lmax, "biorthogonal")
+    b.set_ctas_per_sm(ctas)
+    s = torch.cuda.Stream()
+    b.hierarchize(s)
+    s.synchronize()
+    b.status()
+    O = oracle()
+    for g, x, lv in zip(gs, xs, levels):
+        want = O.hierarchize(x.copy(), lv, lmin, lmax, "biorthogonal")
+        assert np.array_equal(g.cpu().numpy().reshape(want.shape), want), lv
     b.close()

@@ -205,15 +205,22 @@ __device__ __forceinline__ f2 f2_splat(float x) {
   unsigned long long const b = __float_as_uint(x);
   return b | (b << 32);
 }
-// A pair from two raw 32-bit words (x in the low half) and back.
+// A pair from two raw 32-bit words (x in the low half) and back, as
+// register-pair moves (no integer arithmetic).
 __device__ __forceinline__ f2 f2_bits(unsigned x, unsigned y) {
-  return static_cast<f2>(x) | (static_cast<f2>(y) << 32);
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(x), "r"(y));
+  return r;
 }
 __device__ __forceinline__ unsigned f2_lo(f2 r) {
-  return static_cast<unsigned>(r);
+  unsigned x;
+  asm("{\n\t.reg .b32 t;\n\tmov.b64 {%0, t}, %1;\n\t}" : "=r"(x) : "l"(r));
+  return x;
 }
 __device__ __forceinline__ unsigned f2_hi(f2 r) {
-  return static_cast<unsigned>(r >> 32);
+  unsigned y;
+  asm("{\n\t.reg .b32 t;\n\tmov.b64 {t, %0}, %1;\n\t}" : "=r"(y) : "l"(r));
+  return y;
 }
 
 // Two double-float values (h.x + l.x, h.y + l.y).

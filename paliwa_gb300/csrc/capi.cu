@@ -196,9 +196,10 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   if (v.log2_n >= 6) k.mask |= 1 << kChooseStaged32;
   if (R == (1 << v.log2_n) || (last && log2G <= 5))
     k.mask |= 1 << kChooseDirect;
-  if (aligned && ((!last && wide_chunk(v.log2_n) > 0 &&
-                   v.log2_inner >= v.log2_row) ||
-                  (last && log2G <= 5 && v.columns >= (1LL << v.log2_row))))
+  // The wide kernel counts column groups in 32 bits.
+  if (aligned && v.columns < (1LL << 30) &&
+      ((!last && wide_chunk(v.log2_n) > 0 && v.log2_inner >= v.log2_row) ||
+       (last && log2G <= 5 && v.columns >= (1LL << v.log2_row))))
     k.mask |= 1 << kChooseWide;
   if (aligned && !last && R == 16 && log2G >= 3 && log2G <= 8 &&
       v.log2_inner + v.log2_es >=

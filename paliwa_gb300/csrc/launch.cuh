@@ -77,6 +77,9 @@ void launch_r(LiftParams const &p, cudaStream_t s) {
 
 template <class A, int R, class Sched, bool Contig>
 void launch_wide_r(LiftParams const &p, cudaStream_t s) {
+  // The wide kernel counts units (two per tile) in 32 bits.
+  if (p.total_tiles >= (1LL << 30))
+    throw StatusError(2, "wide launch of 2^30 tiles or more");
   static thread_local Occupancy occ;
   launch_persistent(wide_kernel<A, R, kThreads, Sched, Contig>,
                     wide_smem_bytes<A, R, kThreads>(), p, s, occ);

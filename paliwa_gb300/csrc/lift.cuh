@@ -1262,11 +1262,13 @@ template <class A> struct WideStages {
   static constexpr int value = sizeof(typename A::Store) == 16 ? 2 : 3;
 };
 
-// Geometry of one unit for one thread.
+// Geometry of one unit for one thread. Units, tiles and column groups are
+// 32-bit (the planner gives the wide kernel only jobs of under 2^30 columns
+// and launches of under 2^30 tiles); element offsets are 64-bit.
 struct WideUnit {
   long long off;  // element offset of the thread's chunk of its first column
-  long long wfirst;  // first column group of the warp
-  long long groups;  // column groups of the job
+  int wfirst;     // first column group of the warp
+  int groups;     // column groups of the job
   int c;          // chunk index
   int log2ls;     // log2 of the lane distance between chunks of a column
   bool active;    // the warp has at least one column group in range
@@ -1293,7 +1295,7 @@ struct WideBlock {
     return job.log2_inner <= log2cw + 1 && log2cw + 1 < log2gw + log2cw &&
            job.log2_kstride == job.log2_inner &&
            job.log2_astride == job.log2_n + job.log2_inner &&
-           w.wfirst + (1LL << log2gw) <= w.groups &&
+           w.wfirst + (1 << log2gw) <= w.groups &&
            ((job.base | job.dst_base) & 15ull) == 0;
   }
   static __device__ __forceinline__ int swz(int b) {
@@ -1302,19 +1304,18 @@ struct WideBlock {
 };
 
 template <int LOG2R, int LOG2NT, int LOG2CW, bool Contig>
-__device__ __forceinline__ WideUnit wide_unit(LiftJob const &job,
-                                              long long unit, int t) {
+__device__ __forceinline__ WideUnit wide_unit(LiftJob const &job, int unit,
+                                              int t) {
+  static_assert(kTileRounds == 2, "a tile is two units");
   int const lane = t & 31;
   int const log2G = job.log2_n - LOG2R;
   int const log2gw = 5 - log2G;  // column groups per warp
   int const log2CR = LOG2NT - log2G;
-  long long const tile = unit / kTileRounds;
-  int const r = static_cast<int>(unit - tile * kTileRounds);
-  long long const groups = job.columns >> LOG2CW;
-  long long const wfirst =
-      (tile - job.tile_begin) * (static_cast<long long>(kTileRounds)
-                                 << log2CR) +
-      (r << log2CR) + (static_cast<long long>(t >> 5) << log2gw);
+  int const local = (unit >> 1) - static_cast<int>(job.tile_begin);
+  int const r = unit & 1;
+  int const groups = static_cast<int>(job.columns >> LOG2CW);
+  int const wfirst = (local << (log2CR + 1)) + (r << log2CR) +
+                     ((t >> 5) << log2gw);
   WideUnit w;
   w.wfirst = wfirst;
   w.groups = groups;
@@ -1329,12 +1330,13 @@ __device__ __forceinline__ WideUnit wide_unit(LiftJob const &job,
     gl = lane & ((1 << log2gw) - 1);
     w.log2ls = log2gw;
   }
-  long long gg = wfirst + gl;
+  int gg = wfirst + gl;
   w.keep = gg < groups;
   if (!w.keep) gg = groups - 1;
-  long long const gc = gg << LOG2CW;  // first column of the group
+  int const gc = gg << LOG2CW;  // first column of the group
   int const log2B = job.log2_inner;
-  w.off = ((gc >> log2B) << job.log2_astride) + (gc & ((1LL << log2B) - 1)) +
+  w.off = (static_cast<long long>(gc >> log2B) << job.log2_astride) +
+          (gc & ((1 << log2B) - 1)) +
           (static_cast<long long>(w.c) << (LOG2R + job.log2_kstride));
   return w;
 }
@@ -1490,8 +1492,9 @@ __global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
   int const t = threadIdx.x;
   int const lane = t & 31;
   long long const T = p.total_tiles;
-  long long const u0 = T * blockIdx.x / gridDim.x * kTileRounds;
-  long long const u1 = T * (blockIdx.x + 1) / gridDim.x * kTileRounds;
+  int const u0 = static_cast<int>(T * blockIdx.x / gridDim.x * kTileRounds);
+  int const u1 =
+      static_cast<int>(T * (blockIdx.x + 1) / gridDim.x * kTileRounds);
   if (u0 >= u1) return;
   // Job cursors of the copy stream and of the compute stream: both only
   // move forward through the CTA's contiguous range.
@@ -1500,26 +1503,27 @@ __global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
       typename std::conditional<kGlobal, GlobalCursor, JobCursor>::type;
   __shared__ JobSlot wjobs[kGlobal ? 1 : NT / 32][2];
   Cursor jl, jc;
-  jl.init(p, &wjobs[kGlobal ? 0 : t >> 5][0], u0 / kTileRounds, lane);
-  jc.init(p, &wjobs[kGlobal ? 0 : t >> 5][1], u0 / kTileRounds, lane);
-  auto job_of = [&](Cursor &cur, long long unit) -> LiftJob const & {
-    return cur.at(p, unit / kTileRounds, lane);
+  jl.init(p, &wjobs[kGlobal ? 0 : t >> 5][0], u0 >> 1, lane);
+  jc.init(p, &wjobs[kGlobal ? 0 : t >> 5][1], u0 >> 1, lane);
+  auto job_of = [&](Cursor &cur, int unit) -> LiftJob const & {
+    return cur.at(p, unit >> 1, lane);
   };
-  auto stage_base = [&](long long unit) {
-    return smem_raw + static_cast<int>(unit % S) * (SLOT_BYTES * NT);
+  // Unit u uses stage (u - u0) mod S, tracked by counters.
+  auto stage_base = [&](int stage) {
+    return smem_raw + stage * (SLOT_BYTES * NT);
   };
-  auto prefetch = [&](long long unit) {
+  auto prefetch = [&](int unit, int stage) {
     LiftJob const &job = job_of(jl, unit);
     WideUnit const w =
         wide_unit<LOG2R, LOG2NT, LOG2CW, Contig>(job, unit, t);
     if (w.active) {
-      unsigned char *const st = stage_base(unit);
+      unsigned char *const st = stage_base(stage);
       if constexpr (Contig) {
         // Lanes copy consecutive pieces of the warp's block; pieces of
         // lanes past the last column group come from the last group.
         int const log2blk = LOG2CW + job.log2_n;  // elements per group
         E const *const wsrc = reinterpret_cast<E const *>(job.base) +
-                              (w.wfirst << log2blk);
+                              (static_cast<long long>(w.wfirst) << log2blk);
         uint4 *const wslots =
             reinterpret_cast<uint4 *>(st) + (t & ~31) * CP::N;
 #pragma unroll
@@ -1529,7 +1533,8 @@ __global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
           CP::owner_of(b, job.log2_n, owner, pc);
           long long o = static_cast<long long>(b) << CP::LOG2PER;
           long long const over =
-              w.wfirst + (o >> log2blk) - (w.groups - 1);
+              static_cast<long long>(w.wfirst) + (o >> log2blk) -
+              (w.groups - 1);
           if (over > 0) o -= over << log2blk;
           cp_async<16>(wslots + CP::slot(owner, pc), wsrc + o);
         }
@@ -1549,7 +1554,8 @@ __global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
         if (WideBlock::use(job, w, log2gw, LOG2CW)) {
           constexpr int PL = SLOT_BYTES / 16;  // pieces per lane
           constexpr int LOG2E16 = Log2<16 / sizeof(E)>::value;
-          long long const slab0 = (w.wfirst << LOG2CW) >> job.log2_inner;
+          long long const slab0 =
+              (static_cast<long long>(w.wfirst) << LOG2CW) >> job.log2_inner;
           E const *const bsrc = reinterpret_cast<E const *>(job.base) +
                                 (slab0 << job.log2_astride);
 #pragma unroll
@@ -1573,19 +1579,24 @@ __global__ void __launch_bounds__(NT, R >= 16 ? 2 : R == 8 ? 3 : 4)
 
 #pragma unroll
   for (int k = 0; k < S - 1; ++k)
-    if (u0 + k < u1) prefetch(u0 + k); else cp_async_commit();
-  for (long long u = u0; u < u1; ++u) {
+    if (u0 + k < u1) prefetch(u0 + k, k); else cp_async_commit();
+  int cs = 0;          // stage of unit u
+  int ps = S - 1;      // stage of unit u + S - 1
+  for (int u = u0; u < u1; ++u) {
     // Contiguous layout: lanes copy into each other's slots, so every lane
     // must be done reading the stage that the next prefetch overwrites, and
     // must see the other lanes' copies of unit u.
     if constexpr (Contig) __syncwarp();
-    if (u + S - 1 < u1) prefetch(u + S - 1); else cp_async_commit();
+    if (u + S - 1 < u1) prefetch(u + S - 1, ps); else cp_async_commit();
+    ps = ps + 1 == S ? 0 : ps + 1;
     cp_async_wait_group<S - 1>();  // this thread's copies of unit u are in
     if constexpr (Contig) __syncwarp();
+    int const stage = cs;
+    cs = cs + 1 == S ? 0 : cs + 1;
     LiftJob const &job = job_of(jc, u);
     WideUnit const w = wide_unit<LOG2R, LOG2NT, LOG2CW, Contig>(job, u, t);
     if (!w.active) continue;  // the whole warp
-    unsigned char const *const st = stage_base(u);
+    unsigned char const *const st = stage_base(stage);
     V v[R];
     if constexpr (Contig) {
       E el[CW * R];

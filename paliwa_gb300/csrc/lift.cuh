@@ -891,6 +891,44 @@ template <typename S, int R, int NT> struct TileCopy {
     long long const a0 = gc0 >> log2B;
     long long const b0 = gc0 & ((1LL << log2B) - 1);
     long long const columns = job.columns;
+    if ((1 << log2RL) == cols) {
+      // The rows span the tile's columns (one outer slab): every vector of
+      // this thread has the same column q * VW, and its row advances by
+      // dk = NT / (vectors per row) per step, so offsets advance by
+      // constants (modulo the pencil for windows).
+      int const q = t & ((1 << log2vpr) - 1);
+      int const w0 = q * VW;
+      if (gc0 + w0 >= columns) return;
+      int const dk = NT >> log2vpr;
+      int k = t >> log2vpr;
+      long long pk = pos(k);
+      long long const obase = (a0 << job.log2_astride) + b0 + w0;
+      int const sbase = w0 * pitch;
+#pragma unroll 4
+      for (int i = 0; i < PER; ++i) {
+        int const sb = sbase + (k >> LOG2R) * (R + 1) + (k & (R - 1));
+        long long const off = obase + (pk << job.log2_kstride);
+        if constexpr (Store) {
+          if (keep(seg, k, halo, seg_len)) {
+            S tmp[VW];
+#pragma unroll
+            for (int e = 0; e < VW; ++e) tmp[e] = stage[sb + e * pitch];
+            U u;
+            memcpy(&u, tmp, sizeof(U));
+            *reinterpret_cast<U *>(g + off) = u;
+          }
+        } else {
+          S const *const src = source(k) + off;
+#pragma unroll
+          for (int e = 0; e < VW; ++e)
+            cp_async<sizeof(S)>(stage + sb + e * pitch, src + e);
+        }
+        k += dk;
+        pk += dk;
+        if (pk >= n) pk -= n;  // a window wrapping around the period
+      }
+      return;
+    }
     auto locate = [&](int v, long long &off, int &sb, int &k) -> bool {
       int const rho = v >> log2vpr;
       int const q = v & ((1 << log2vpr) - 1);
@@ -1134,7 +1172,8 @@ __device__ __forceinline__ void lift_body(LiftParams const &p) {
     long long const n = 1LL << job->log2_n;
 
     long long const local = tile - job->tile_begin;
-    long long const seg = local / job->col_tiles;
+    // A periodic job has one segment (no 64-bit division per tile).
+    long long const seg = periodic ? 0 : local / job->col_tiles;
     long long const gc0 = (local - seg * job->col_tiles) * cols;
     long long const wstart =
         periodic ? 0 : seg * job->seg_len - job->halo;  // window origin
@@ -1817,13 +1856,18 @@ __global__ void __launch_bounds__(NT, 2)
     unsigned char *const st = smem_raw + buf * STAGE;
     E const *const src = reinterpret_cast<E const *>(job.base);
     int const log2q = g.log2rb - g.log2pb;  // pieces per row
-    int const pieces = 1 << (job.log2_n + log2q);
     int const cols_q = g.log2pb - LOG2ES;   // log2 columns per piece
-    for (int i = t; i < pieces; i += NT) {
-      int const k = i >> log2q;
-      int const q = i & ((1 << log2q) - 1);
-      E const *const from = src + elem(job, g, static_cast<long long>(q)
-                                                    << cols_q, k);
+    // Piece i = t + j NT is row k = i >> log2q, piece q = i mod 2^log2q of
+    // the row; a row has at most NT pieces, so q is the same for all of a
+    // thread's pieces and k advances by NT >> log2q.
+    int const q = t & ((1 << log2q) - 1);
+    int const dk = NT >> log2q;
+    E const *const from0 =
+        src + elem(job, g, static_cast<long long>(q) << cols_q, 0);
+    int const n = 1 << job.log2_n;
+    for (int k = t >> log2q; k < n; k += dk) {
+      E const *const from = from0 + (static_cast<long long>(k)
+                                     << job.log2_kstride);
       if (g.log2pb == 4)
         cp_async<16>(st + smem_off(g, k, q), from);
       else
@@ -1873,19 +1917,23 @@ __global__ void __launch_bounds__(NT, 2)
     __syncthreads();  // the transformed tile is in shared memory
     E *const dst = reinterpret_cast<E *>(job.dst_base);
     int const log2q = g.log2rb - g.log2pb;
-    int const pieces = 1 << (job.log2_n + log2q);
     int const cols_q = g.log2pb - LOG2ES;
-    for (int i = t; i < pieces; i += NT) {
-      int const k = i >> log2q;
-      int const q = i & ((1 << log2q) - 1);
-      long long const tc = static_cast<long long>(q) << cols_q;
-      if (g.gc0 + tc >= g.columns) continue;
-      unsigned char const *const from = st + smem_off(g, k, q);
-      E *const to = dst + elem(job, g, tc, k);
-      if (g.log2pb == 4)
-        *reinterpret_cast<uint4 *>(to) = *reinterpret_cast<uint4 const *>(from);
-      else
-        *reinterpret_cast<uint2 *>(to) = *reinterpret_cast<uint2 const *>(from);
+    int const q = t & ((1 << log2q) - 1);  // as in the copy in
+    long long const tc = static_cast<long long>(q) << cols_q;
+    if (g.gc0 + tc < g.columns) {
+      int const dk = NT >> log2q;
+      E *const to0 = dst + elem(job, g, tc, 0);
+      int const n = 1 << job.log2_n;
+      for (int k = t >> log2q; k < n; k += dk) {
+        unsigned char const *const from = st + smem_off(g, k, q);
+        E *const to = to0 + (static_cast<long long>(k) << job.log2_kstride);
+        if (g.log2pb == 4)
+          *reinterpret_cast<uint4 *>(to) =
+              *reinterpret_cast<uint4 const *>(from);
+        else
+          *reinterpret_cast<uint2 *>(to) =
+              *reinterpret_cast<uint2 const *>(from);
+      }
     }
   }
   cp_async_wait_all();

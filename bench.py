@@ -628,12 +628,23 @@ def run_gpu(args, w, world, rank, local):
     del b32, v32
     link = measure_link(host_in, host_out, hb.buf)
 
+    # Events after every step, for the per-step times reported beside the
+    # total (the total is what `value` uses).
+    step_events = []
+
     def e2e_step():
         hb.run(host_in, host_out, stream=stream)
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record(stream)
+        step_events.append(ev)
 
     with torch.cuda.stream(stream):
         e2e_ms = time_steps(e2e_step, lambda: None, max(1, args.steps // 2),
                             args.warmup, stream, world)
+    k_e2e = max(1, args.steps // 2)
+    timed_events = step_events[-(k_e2e + 1):]
+    e2e_step_ms = [a.elapsed_time(b) for a, b in
+                   zip(timed_events[:-1], timed_events[1:])]
     e2e_ms = max_over_ranks(world, e2e_ms)
     e2e_value = pts_step * max(1, args.steps // 2) / (e2e_ms / 1e3)
     e2e_bytes = hb.numel() * 4
@@ -708,7 +719,8 @@ def run_gpu(args, w, world, rank, local):
                     "h2d_bytes_per_step": e2e_bytes,
                     "d2h_bytes_per_step": e2e_bytes,
                     "groups": E2E_GROUPS, "host_numa_node": numa,
-                    "link": link},
+                    "link": link,
+                    "step_ms_after_first": [round(x, 2) for x in e2e_step_ms]},
             "gpu_launches": args.steps * nlaunch,
             "cpu_baseline": cpu,
         }

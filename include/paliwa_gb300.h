@@ -255,6 +255,17 @@ int paliwa_gb_batch_set_groups(paliwa_gb_batch *batch, int ngroups);
  * directions after synchronizing the device. No counterpart in the
  * reference. */
 int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable);
+/* enable != 0 (default): FP32-compensated strided stages that the wide
+ * kernel takes (pencils of up to 64 points, inner extent of 4 or more
+ * columns, 16-byte aligned grids) run on the TMA wide kernel: the same
+ * register transform, with each tile of columns moved between HBM and
+ * shared memory by bulk tensor copies over a tensor map of the grid's axis
+ * (bounded waits, reported by paliwa_gb_batch_status); 0 keeps the wide
+ * kernel's per-thread copies. Results are the same bits either way.
+ * Re-plans both directions after synchronizing the device; the autotuner
+ * keeps whichever is faster per direction. No counterpart in the
+ * reference. */
+int paliwa_gb_batch_use_tma(paliwa_gb_batch *batch, int enable);
 /* ctas > 0 caps every launch of the batch at that many CTAs per SM (the
  * kernels are persistent: by default a launch takes every slot that fits),
  * which leaves room on each SM for the launches of the batch's other
@@ -280,7 +291,7 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
  * (its bytes count one read and one write of each point it copies), 1024
  * the slab kernel (every level of a grid's
  * trailing axes in one pass; its bytes count one read and one write of each
- * point); `kernels` may be null. Call with
+ * point), 2048 + R the TMA wide kernel; `kernels` may be null. Call with
  * capacity 0 to get *nlaunches first. */
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,

@@ -62,6 +62,7 @@ SIGNATURES = {
     "paliwa_gb_batch_use_slabs": (_i, [_vp, _i]),
     "paliwa_gb_batch_status": (_i, [_vp]),
     "paliwa_gb_batch_set_ctas_per_sm": (_i, [_vp, _i]),
+    "paliwa_gb_batch_use_tma": (_i, [_vp, _i]),
     "paliwa_gb_batch_create": (
         _i, [_i, _i, _pi64, _pi64, _pi64, _i, _i, ctypes.POINTER(_vp),
              ctypes.POINTER(_vp)]),

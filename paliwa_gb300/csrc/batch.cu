@@ -27,11 +27,14 @@
 #include "paliwa_gb300.h"
 #include "plan.hpp"
 #include "slab.cuh"
+#include "twide.cuh"
 
 namespace pgb {
 void launch_slab_f64(int sched, SlabParams const &p, cudaStream_t s);
 void launch_slab_f32(int sched, SlabParams const &p, cudaStream_t s);
 void launch_slab_f32c(int sched, SlabParams const &p, cudaStream_t s);
+void launch_twide_f32c(int sched, int R, TWideParams const &p,
+                       cudaStream_t s);
 } // namespace pgb
 
 using namespace pgb;
@@ -43,8 +46,10 @@ namespace {
 // group, 26.1 with two, 25.7 with three, 25.6 with four.
 constexpr int kBatchGroups = 4;
 
-// Kernel code of a slab launch (slab.cuh); the others are plan.hpp's.
+// Kernel code of a slab launch (slab.cuh) and, plus the chunk size, of a
+// TMA wide launch (twide.cuh); the others are plan.hpp's.
 constexpr int kSlab = 1024;
+constexpr int kTWide = 2048;
 
 struct Launch {
   int group = 0;
@@ -65,11 +70,18 @@ struct Direction {
   LiftJob *jobs_dev = nullptr;
   SlabJob *slab_dev = nullptr;  // jobs of the slab launches
   int *slab_tile_dev = nullptr;  // job of every tile of the slab launches
+  // TMA wide launches: jobs, the job of every tile, the tensor maps.
+  TWideJob *twide_dev = nullptr;
+  int *twide_tile_dev = nullptr;
+  CUtensorMap *maps_dev = nullptr;
   cudaGraphExec_t graph = nullptr;
   Tuning tuning;  // kernel forced per class (autotuner)
   // Slab launches where they apply (the batch's setting); the autotuner
   // clears it when the direction runs faster axis by axis.
   bool slabs = true;
+  // TMA wide launches for the strided wide stages (the batch's setting);
+  // the autotuner may clear it per direction.
+  bool tma = true;
   // Classes of the plan's periodic stages: applicable kernels (bits), the
   // default choice of the first stage seen, and the points they store.
   struct ClassInfo {
@@ -85,7 +97,13 @@ void free_direction(Direction &d) {
   if (d.jobs_dev) cudaFree(d.jobs_dev);
   if (d.slab_dev) cudaFree(d.slab_dev);
   if (d.slab_tile_dev) cudaFree(d.slab_tile_dev);
+  if (d.twide_dev) cudaFree(d.twide_dev);
+  if (d.twide_tile_dev) cudaFree(d.twide_tile_dev);
+  if (d.maps_dev) cudaFree(d.maps_dev);
   d.slab_tile_dev = nullptr;
+  d.twide_dev = nullptr;
+  d.twide_tile_dev = nullptr;
+  d.maps_dev = nullptr;
   d.graph = nullptr;
   d.jobs_dev = nullptr;
   d.slab_dev = nullptr;
@@ -144,6 +162,8 @@ struct paliwa_gb_batch {
   // Slab launches (slab.cuh): the tensor map over the grids' memory as
   // 128-byte rows from slab_base, and the error word of their bounded waits.
   bool use_slabs = true;
+  // TMA wide launches for strided wide stages of FP32c grids.
+  bool use_tma = true;
   bool slab_map_ok = false;
   unsigned long long slab_base = 0;
   CUtensorMap slab_map{};
@@ -251,6 +271,69 @@ bool encode_slab_map(CUtensorMap *map, unsigned long long base,
   return r == CUDA_SUCCESS;
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (encode == nullptr) {
+    cudaDriverEntryPointQueryResult q{};
+    void *fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                         cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || fn == nullptr)
+      return nullptr;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  return encode;
+}
+
+// Stage codes of the strided wide kernel that the TMA wide kernel takes.
+bool twide_code(int R) {
+  return R == kWide + 2 || R == kWide + 4 || R == kWide + 8 ||
+         R == kWide + 16;
+}
+
+// The TMA wide job and tensor map of a strided wide stage (FP32c, float
+// storage): the 3D view [outer][n][inner] of the stage's pencils with the
+// axis' strides, boxes {Bx, n, Sx} covering one tile of Ct = 2 NT / G
+// columns. False when the stage does not qualify (alignment, inner extent
+// under 4 columns, 2^30 tiles or more, or the encoder refuses the map).
+bool twide_job(Stage const &st, TWideJob &job, CUtensorMap &map,
+               long long &tiles) {
+  auto encode = tensor_map_encoder();
+  LiftJob const &lj = st.job;
+  int const r = st.R - kWide;
+  int const log2r = 31 - __builtin_clz(static_cast<unsigned>(r));
+  int const log2G = lj.log2_n - log2r;
+  if (encode == nullptr || lj.periodic != 1 || lj.base % 16 != 0 ||
+      lj.log2_inner < 2 || log2G < 0 || log2G > 2 || lj.log2_n > 6)
+    return false;
+  int const log2ct = Log2<kTWideThreads>::value + 1 - log2G;
+  std::memset(&job, 0, sizeof(job));
+  job.log2_n = lj.log2_n;
+  job.log2_inner = lj.log2_inner;
+  job.nlevels = lj.nlevels;
+  job.log2_bx = std::min(std::min(lj.log2_inner, log2ct), 8);
+  job.log2_sx = std::max(0, log2ct - lj.log2_inner);
+  job.nxb = 1 << (log2ct - job.log2_bx - job.log2_sx);
+  tiles = (lj.columns + (1LL << log2ct) - 1) >> log2ct;
+  if (tiles >= (1LL << 30)) return false;
+  long long const outer = lj.columns >> lj.log2_inner;
+  cuuint64_t dims[3] = {static_cast<cuuint64_t>(1) << lj.log2_inner,
+                        static_cast<cuuint64_t>(1) << lj.log2_n,
+                        static_cast<cuuint64_t>(outer)};
+  cuuint64_t strides[2] = {static_cast<cuuint64_t>(4) << lj.log2_kstride,
+                           static_cast<cuuint64_t>(4) << lj.log2_astride};
+  cuuint32_t box[3] = {1u << job.log2_bx, 1u << lj.log2_n,
+                       1u << job.log2_sx};
+  cuuint32_t elem[3] = {1, 1, 1};
+  CUresult const res = encode(
+      &map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+      reinterpret_cast<void *>(lj.base), dims, strides, box, elem,
+      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return res == CUDA_SUCCESS;
+}
+
 // The tensor map over every grid of the batch (rows of 128 bytes from the
 // lowest grid address, rounded down to 128 bytes).
 void setup_slab_map(paliwa_gb_batch &b) {
@@ -279,8 +362,13 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
   std::vector<LiftJob> all_jobs;
   std::vector<SlabJob> all_slabs;
   std::vector<int> slab_tiles;  // per slab launch tile: its job in the launch
+  std::vector<TWideJob> all_twide;
+  std::vector<int> twide_tiles;  // per TMA wide launch tile: its job
+  std::vector<CUtensorMap> maps;
   size_t const es = dtype_size(b.dtype);
   int const ws = wavelet_schedule(filters);
+  bool const tma = b.use_tma && dr.tma && b.dtype == PALIWA_GB_F32C &&
+                   ws >= 0 && tensor_map_encoder() != nullptr;
   // First axis of every grid's slab group (ndim: none).
   std::vector<int> slab_from(b.ngrids, b.ndim);
   if (b.use_slabs && dr.slabs && b.slab_map_ok && ws >= 0)
@@ -326,12 +414,63 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
         depth = std::max(depth, stages[i].size());
       }
       for (size_t k = 0; k < depth; ++k) {
-        // One launch per chunk size among the k-th stages of the group.
+        // One launch per chunk size among the k-th stages of the group;
+        // strided wide stages that qualify go to the TMA wide kernel.
         std::map<int, std::vector<Stage const *>> by_r;
         for (size_t i = 0; i < members.size(); ++i)
-          if (k < stages[i].size())
-            by_r[stages[i][k].R].push_back(&stages[i][k]);
+          if (k < stages[i].size()) {
+            Stage const &st = stages[i][k];
+            int code = st.R;
+            if (tma && twide_code(st.R) &&
+                canonical_shifts(st.job, (ws & 1) != 0))
+              code = kTWide + (st.R - kWide);
+            by_r[code].push_back(&st);
+          }
         for (auto const &[R, list] : by_r) {
+          if (R > kTWide) {
+            Launch L;
+            L.group = grp;
+            L.R = R;
+            L.sched = ws;
+            L.job_first = all_twide.size();
+            L.tile_first = twide_tiles.size();
+            std::vector<Stage const *> rest;  // stages that do not qualify
+            for (Stage const *st : list) {
+              TWideJob job;
+              CUtensorMap map;
+              long long tiles = 0;
+              if (!twide_job(*st, job, map, tiles)) {
+                rest.push_back(st);
+                continue;
+              }
+              job.tile_begin = L.tiles;
+              job.map = static_cast<int>(maps.size());
+              maps.push_back(map);
+              all_twide.push_back(job);
+              twide_tiles.insert(twide_tiles.end(), tiles, L.njobs);
+              L.tiles += tiles;
+              L.points += stage_points(*st);
+              ++L.njobs;
+            }
+            if (L.njobs > 0) dr.launches.push_back(L);
+            if (rest.empty()) continue;
+            // The rest on the wide kernel.
+            Launch W;
+            W.group = grp;
+            W.R = kWide + (R - kTWide);
+            W.sched = ws;
+            W.job_first = all_jobs.size();
+            W.njobs = static_cast<int>(rest.size());
+            for (Stage const *st : rest) {
+              LiftJob job = st->job;
+              job.tile_begin = W.tiles;
+              W.tiles += st->tiles;
+              W.points += stage_points(*st);
+              all_jobs.push_back(job);
+            }
+            dr.launches.push_back(W);
+            continue;
+          }
           Launch L;
           L.group = grp;
           L.R = R;
@@ -387,6 +526,23 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
                           cudaMemcpyHostToDevice),
                "cudaMemcpy(slab tiles)");
   }
+  if (!all_twide.empty()) {
+    size_t const jb = all_twide.size() * sizeof(TWideJob);
+    cuda_check(cudaMalloc(&dr.twide_dev, jb), "cudaMalloc(twide jobs)");
+    cuda_check(cudaMemcpy(dr.twide_dev, all_twide.data(), jb,
+                          cudaMemcpyHostToDevice),
+               "cudaMemcpy(twide jobs)");
+    size_t const tb = twide_tiles.size() * sizeof(int);
+    cuda_check(cudaMalloc(&dr.twide_tile_dev, tb), "cudaMalloc(twide tiles)");
+    cuda_check(cudaMemcpy(dr.twide_tile_dev, twide_tiles.data(), tb,
+                          cudaMemcpyHostToDevice),
+               "cudaMemcpy(twide tiles)");
+    size_t const mb = maps.size() * sizeof(CUtensorMap);
+    cuda_check(cudaMalloc(&dr.maps_dev, mb), "cudaMalloc(tensor maps)");
+    cuda_check(cudaMemcpy(dr.maps_dev, maps.data(), mb,
+                          cudaMemcpyHostToDevice),
+               "cudaMemcpy(tensor maps)");
+  }
   if (!all_jobs.empty()) {
     size_t const bytes = all_jobs.size() * sizeof(LiftJob);
     cuda_check(cudaMalloc(&dr.jobs_dev, bytes), "cudaMalloc(jobs)");
@@ -399,6 +555,18 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
 // One launch of a direction's plan: a lifting kernel or a slab kernel.
 void launch_one(paliwa_gb_batch &b, Direction &dr, Launch const &L,
                 cudaStream_t s) {
+  if (L.R > kTWide) {
+    TWideParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.maps = dr.maps_dev;
+    p.jobs = dr.twide_dev + L.job_first;
+    p.tile_job = dr.twide_tile_dev + L.tile_first;
+    p.total_tiles = L.tiles;
+    p.error = b.slab_error;
+    p.ctas_per_sm = b.ctas_per_sm;
+    launch_twide_f32c(L.sched, L.R - kTWide, p, s);
+    return;
+  }
   if (L.R != kSlab) {
     LiftParams lp = dr.params;
     lp.ctas_per_sm = b.ctas_per_sm;
@@ -852,6 +1020,16 @@ int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable) {
   });
 }
 
+int paliwa_gb_batch_use_tma(paliwa_gb_batch *batch, int enable) {
+  return guarded([&] {
+    if (batch == nullptr)
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null batch");
+    cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    batch->use_tma = enable != 0;
+    setup_groups(*batch, batch->ngroups);
+  });
+}
+
 int paliwa_gb_batch_set_ctas_per_sm(paliwa_gb_batch *batch, int ctas) {
   return guarded([&] {
     if (batch == nullptr || ctas < 0)
@@ -959,6 +1137,21 @@ int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,
           ++nchanged;
         } else {
           dr.slabs = !dr.slabs;
+          replan(*batch, which);
+        }
+      }
+      // TMA wide launches against the wide kernel's own copies.
+      bool has_twide = false;
+      for (auto const &L : dr.launches) has_twide |= L.R > kTWide;
+      if (batch->use_tma && (has_twide || !dr.tma)) {
+        dr.tma = !dr.tma;
+        replan(*batch, which);
+        float const t = time_direction(*batch, which, reps, s);
+        if (t < best * 0.99f) {
+          best = t;
+          ++nchanged;
+        } else {
+          dr.tma = !dr.tma;
           replan(*batch, which);
         }
       }

@@ -1,0 +1,66 @@
+// Launches of the TMA wide kernel (twide.cuh) for FP32-compensated grids
+// (rows of two columns as double-float f32x2 pairs).
+#include "launch.cuh"
+#include "twide.cuh"
+
+namespace pgb {
+
+namespace {
+
+template <int R, class Sched>
+void launch_twide_r(TWideParams const &p, cudaStream_t s) {
+  static thread_local Occupancy occ;
+  auto kernel = twide_kernel<RowF32C, R, Sched>;
+  size_t const smem = twide_smem_bytes<R>();
+  int const dev = current_device();
+  if (dev < 0 || dev >= Occupancy::kMaxDevices)
+    throw StatusError(2, "device ordinal beyond the launch cache");
+  int &per_sm = occ.per_sm[dev];
+  int &sms = occ.sms[dev];
+  if (per_sm == 0) {
+    cuda_check(cudaFuncSetAttribute(
+                   kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                   static_cast<int>(smem)),
+               "cudaFuncSetAttribute(twide)");
+    int n = 0;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &n, kernel, kTWideThreads, smem),
+               "occupancy query (twide)");
+    sms = device_sms();
+    per_sm = n < 1 ? 1 : n;
+  }
+  long long const resident =
+      static_cast<long long>(capped_per_sm(per_sm, p.ctas_per_sm)) * sms;
+  long long const blocks = std::min(p.total_tiles, resident);
+  kernel<<<static_cast<unsigned>(blocks), kTWideThreads, smem, s>>>(p);
+  cuda_check(cudaGetLastError(), "twide kernel launch");
+}
+
+template <class Sched>
+void by_r(int R, TWideParams const &p, cudaStream_t s) {
+  switch (R) {
+  case 2: return launch_twide_r<2, Sched>(p, s);
+  case 4: return launch_twide_r<4, Sched>(p, s);
+  case 8: return launch_twide_r<8, Sched>(p, s);
+  case 16: return launch_twide_r<16, Sched>(p, s);
+  }
+  throw StatusError(2, "twide launch with an unsupported chunk size");
+}
+
+} // namespace
+
+// sched = 2 * wavelet + (forward ? 1 : 0); R = rows per chunk.
+void launch_twide_f32c(int sched, int R, TWideParams const &p,
+                       cudaStream_t s) {
+  switch (sched) {
+  case 0: return by_r<WaveletSched<0, false>>(R, p, s);
+  case 1: return by_r<WaveletSched<0, true>>(R, p, s);
+  case 2: return by_r<WaveletSched<1, false>>(R, p, s);
+  case 3: return by_r<WaveletSched<1, true>>(R, p, s);
+  case 4: return by_r<WaveletSched<2, false>>(R, p, s);
+  case 5: return by_r<WaveletSched<2, true>>(R, p, s);
+  }
+  throw StatusError(2, "twide kernel planned without a wavelet schedule");
+}
+
+} // namespace pgb

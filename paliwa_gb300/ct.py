@@ -68,12 +68,16 @@ def packed_grids(levels, dtype, device="cuda", align=64):
     return buf, [buf.narrow(0, o, s) for o, s in zip(offsets, sizes)]
 
 
-# Launch code of the slab kernel in Batch.profile.
+# Launch codes of the slab kernel and (plus the chunk size) of the TMA wide
+# kernel in Batch.profile.
 SLAB_KERNEL = 1024
+TWIDE_KERNEL = 2048
 
 
 def kernel_name(code):
     """Name of the lifting kernel behind a launch code of Batch.profile."""
+    if code > TWIDE_KERNEL:
+        return f"twide_kernel R={code - TWIDE_KERNEL}"
     if code == SLAB_KERNEL:
         return "slab_kernel"
     if code == 512:
@@ -145,6 +149,12 @@ class Batch:
         slab launch (default), or every axis on its own (the same bits).
         Synchronizes the device."""
         _lib.check(self._lib.paliwa_gb_batch_use_slabs(self._h, int(enable)))
+
+    def use_tma(self, enable):
+        """Run the FP32c strided stages of the wide kernel on the TMA wide
+        kernel (default), or on the wide kernel's per-thread copies (the
+        same bits). Synchronizes the device."""
+        _lib.check(self._lib.paliwa_gb_batch_use_tma(self._h, int(enable)))
 
     def set_ctas_per_sm(self, ctas):
         """Cap every launch of the batch at ``ctas`` CTAs per SM, leaving

@@ -443,3 +443,46 @@ def test_ctas_per_sm_cap_gives_identical_results(ctas):
         want = O.hierarchize(x.copy(), lv, lmin, lmax, "biorthogonal")
         assert np.array_equal(g.cpu().numpy().reshape(want.shape), want), lv
     b.close()
+
+
+def test_tma_wide_kernel_gives_the_wide_kernels_bits():
+    """FP32-compensated strided stages of up to 64 points run on the TMA
+    wide kernel by default; the per-thread-copy wide kernel gives the same
+    bits, forward and inverse, for every wavelet. The scheme mixes inner
+    extents of 2 columns (left on the wide kernel), 4 to 2^10 columns, grids
+    smaller than one tile and sub-lattice stages of long pencils."""
+    import torch
+    levels = [(6, 1, 3), (5, 2, 2), (4, 6, 1), (3, 3, 5), (6, 6, 2), (2, 5, 7),
+              (1, 4, 9), (6, 2, 1), (2, 2, 2), (14, 2, 1), (5, 5, 5),
+              (4, 1, 10)]
+    lmin, lmax = (1, 1, 1), (14, 14, 14)
+    rng = np.random.default_rng(77)
+    host = [rng.uniform(-1, 1, 1 << sum(l)).astype(np.float32)
+            for l in levels]
+    for wavelet in ("hat", "biorthogonal", "fullweighting"):
+        out = []
+        for tma in (True, False):
+            buf, gs = pct.packed_grids(levels, torch.float32)
+            for g, h in zip(gs, host):
+                g.copy_(torch.from_numpy(h))
+            b = pct.Batch(gs, levels, lmin, lmax, wavelet, compensated=True)
+            if not tma:
+                b.use_tma(False)
+            s = torch.cuda.Stream()
+            kernels = b.profile(True, stream=s)[2]
+            if tma:
+                assert any(k > pct.TWIDE_KERNEL for k in kernels)
+            else:
+                assert not any(k > pct.TWIDE_KERNEL for k in kernels)
+            for g, h in zip(gs, host):
+                g.copy_(torch.from_numpy(h))
+            b.hierarchize(s)
+            s.synchronize()
+            fwd = buf.clone()
+            b.dehierarchize(s)
+            s.synchronize()
+            b.status()
+            out.append((fwd, buf.clone()))
+            b.close()
+        assert torch.equal(out[0][0], out[1][0]), wavelet
+        assert torch.equal(out[0][1], out[1][1]), wavelet

@@ -308,6 +308,9 @@ bool twide_job(Stage const &st, TWideJob &job, CUtensorMap &map,
       lj.log2_inner < 2 || log2G < 0 || log2G > 2 || lj.log2_n > 6)
     return false;
   int const log2ct = Log2<kTWideThreads>::value + 1 - log2G;
+  // Units per tile: TWideShape<R>::kUnits (16 KB tiles for chunks of up to
+  // 8 points).
+  int const log2u = r >= 8 ? 0 : 3 - log2r;
   std::memset(&job, 0, sizeof(job));
   job.log2_n = lj.log2_n;
   job.log2_inner = lj.log2_inner;
@@ -315,7 +318,7 @@ bool twide_job(Stage const &st, TWideJob &job, CUtensorMap &map,
   job.log2_bx = std::min(std::min(lj.log2_inner, log2ct), 8);
   job.log2_sx = std::max(0, log2ct - lj.log2_inner);
   job.nxb = 1 << (log2ct - job.log2_bx - job.log2_sx);
-  tiles = (lj.columns + (1LL << log2ct) - 1) >> log2ct;
+  tiles = (lj.columns + (1LL << (log2ct + log2u)) - 1) >> (log2ct + log2u);
   if (tiles >= (1LL << 30)) return false;
   long long const outer = lj.columns >> lj.log2_inner;
   cuuint64_t dims[3] = {static_cast<cuuint64_t>(1) << lj.log2_inner,

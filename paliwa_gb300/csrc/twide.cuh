@@ -79,13 +79,26 @@ __device__ __forceinline__ void fence_tensormap(void const *map) {
                : "memory");
 }
 
-// Bytes of one tile: Ct * n * 4 = (2 NT / G) * (G R) * 4; tiles in flight.
+// A tile is kUnits units of Ct * n * 4 = (2 NT / G) * (G R) * 4 bytes
+// (16 KB tiles for chunks of up to 8 points: per-tile synchronisation
+// dominated 8 KB ones). kStages tiles per CTA: one transformed, kLook
+// loading ahead, and kDefer whose stores may still be reading shared memory
+// when a buffer is reloaded (so the reload does not wait for the store just
+// issued).
 template <int R> struct TWideShape {
-  static constexpr int kTileBytes = 8 * kTWideThreads * R;
+  static constexpr int kUnits = R >= 8 ? 1 : 8 / R;
+  static constexpr int kUnitBytes = 8 * kTWideThreads * R;
+  static constexpr int kTileBytes = kUnits * kUnitBytes;
   static constexpr int kStages = R >= 16 ? 3 : 4;
+  static constexpr int kDefer = R >= 16 ? 0 : 1;
+  static constexpr int kLook = kStages - 1 - kDefer;
   static constexpr size_t kSmemBytes =
       size_t(kStages) * kTileBytes + 128;  // + 128-byte alignment slack
 };
+
+__device__ __forceinline__ void bulk_wait_read_1() {
+  asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
+}
 template <int R> constexpr size_t twide_smem_bytes() {
   return TWideShape<R>::kSmemBytes;
 }
@@ -99,6 +112,10 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
   constexpr int NT = kTWideThreads;
   constexpr int S = TWideShape<R>::kStages;
   constexpr int TILE = TWideShape<R>::kTileBytes;
+  constexpr int U = TWideShape<R>::kUnits;
+  constexpr int UNIT = TWideShape<R>::kUnitBytes;
+  constexpr int LOOK = TWideShape<R>::kLook;
+  constexpr int DEFER = TWideShape<R>::kDefer;
   constexpr int LOG2R = Log2<R>::value;
   constexpr int LOG2NT = Log2<NT>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -121,10 +138,12 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
   }
   __syncthreads();
 
-  // Tile `tile` of `job`: its first column's (inner, outer) coordinates.
-  auto origin = [](TWideJob const &job, long long tile, int &x0, int &z0) {
+  // Unit u of tile `tile` of `job`: its first column's (inner, outer)
+  // coordinates.
+  auto origin = [](TWideJob const &job, long long tile, int u, int &x0,
+                   int &z0) {
     int const log2ct = LOG2NT + 1 - (job.log2_n - LOG2R);
-    long long const col0 = (tile - job.tile_begin) << log2ct;
+    long long const col0 = ((tile - job.tile_begin) * U + u) << log2ct;
     z0 = static_cast<int>(col0 >> job.log2_inner);
     x0 = static_cast<int>(col0 & ((1LL << job.log2_inner) - 1));
   };
@@ -155,15 +174,17 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
       fence_tensormap(map);
       fenced = job.map;
     }
-    int x0, z0;
-    origin(job, tile, x0, z0);
     int const bb = box_bytes(job);
-    mbar_expect_tx(&full[b], static_cast<unsigned>(bb * job.nxb));
-    unsigned char *const dst = tiles + b * TILE;
-    for (int xb = 0; xb < job.nxb; ++xb) {
-      int x, z;
-      box_at(job, xb, x0, z0, x, z);
-      tma_load_3d(dst + xb * bb, map, x, 0, z, &full[b]);
+    mbar_expect_tx(&full[b], static_cast<unsigned>(U * bb * job.nxb));
+    for (int u = 0; u < U; ++u) {
+      int x0, z0;
+      origin(job, tile, u, x0, z0);
+      unsigned char *const dst = tiles + b * TILE + u * UNIT;
+      for (int xb = 0; xb < job.nxb; ++xb) {
+        int x, z;
+        box_at(job, xb, x0, z0, x, z);
+        tma_load_3d(dst + xb * bb, map, x, 0, z, &full[b]);
+      }
     }
   };
   auto issue_store = [&](long long k) {
@@ -171,29 +192,36 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
     long long const tile = first + k * step;
     TWideJob const &job = sjob[b];
     void const *const map = p.maps + job.map;
-    int x0, z0;
-    origin(job, tile, x0, z0);
     int const bb = box_bytes(job);
-    unsigned char const *const src = tiles + b * TILE;
-    for (int xb = 0; xb < job.nxb; ++xb) {
-      int x, z;
-      box_at(job, xb, x0, z0, x, z);
-      tma_store_3d(map, x, 0, z, src + xb * bb);
+    for (int u = 0; u < U; ++u) {
+      int x0, z0;
+      origin(job, tile, u, x0, z0);
+      unsigned char const *const src = tiles + b * TILE + u * UNIT;
+      for (int xb = 0; xb < job.nxb; ++xb) {
+        int x, z;
+        box_at(job, xb, x0, z0, x, z);
+        tma_store_3d(map, x, 0, z, src + xb * bb);
+      }
     }
     bulk_commit();
   };
 
   long long issued = 0;
   if (t == 0)
-    for (; issued < S - 1 && issued < ntiles; ++issued) issue_load(issued);
+    for (; issued < LOOK && issued < ntiles; ++issued) issue_load(issued);
 
   long long k = 0;
   bool failed = false;
   for (; k < ntiles; ++k) {
     int const b = static_cast<int>(k % S);
     if (t == 0 && issued < ntiles) {
-      // The buffer of tile k - 1: its stores must have read it.
-      bulk_wait_read_all();
+      // The buffer of tile k + LOOK held tile k + LOOK - S = k - 1 - DEFER:
+      // its stores (all but the DEFER most recent store groups) must have
+      // read it.
+      if constexpr (DEFER == 0)
+        bulk_wait_read_all();
+      else
+        bulk_wait_read_1();
       issue_load(issued);
       ++issued;
     }
@@ -222,21 +250,25 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
     int const s = rem >> job.log2_bx;
     int const bcol = rem & ((1 << job.log2_bx) - 1);
     // float index of row c R of the thread's columns; rows are Bx apart
-    float *const tf = reinterpret_cast<float *>(tiles + b * TILE);
     int const idx0 = (xb << (log2bs + job.log2_n)) +
                      ((((s << job.log2_n) + (c << LOG2R)) << job.log2_bx) +
                       bcol);
-    V v[R];
+    for (int u = 0; u < U; ++u) {
+      float *const tf =
+          reinterpret_cast<float *>(tiles + b * TILE + u * UNIT);
+      V v[R];
 #pragma unroll
-    for (int j = 0; j < R; ++j)
-      v[j] = A::load(
-          *reinterpret_cast<W const *>(tf + idx0 + (j << job.log2_bx)));
-    RoundCtx<A, NT> ctx(t, c, 1 << log2G, log2G, lane, 1, nullptr, nullptr,
-                        log2W);
-    Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
+      for (int j = 0; j < R; ++j)
+        v[j] = A::load(
+            *reinterpret_cast<W const *>(tf + idx0 + (j << job.log2_bx)));
+      RoundCtx<A, NT> ctx(t, c, 1 << log2G, log2G, lane, 1, nullptr, nullptr,
+                          log2W);
+      Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
 #pragma unroll
-    for (int j = 0; j < R; ++j)
-      *reinterpret_cast<W *>(tf + idx0 + (j << job.log2_bx)) = A::store(v[j]);
+      for (int j = 0; j < R; ++j)
+        *reinterpret_cast<W *>(tf + idx0 + (j << job.log2_bx)) =
+            A::store(v[j]);
+    }
     fence_proxy_async_smem();
     __syncthreads();
     if (t == 0) issue_store(k);

@@ -260,10 +260,11 @@ int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable);
  * columns, 16-byte aligned grids) run on the TMA wide kernel: the same
  * register transform, with each tile of columns moved between HBM and
  * shared memory by bulk tensor copies over a tensor map of the grid's axis
- * (bounded waits, reported by paliwa_gb_batch_status); 0 keeps the wide
- * kernel's per-thread copies. Results are the same bits either way.
- * Re-plans both directions after synchronizing the device; the autotuner
- * keeps whichever is faster per direction. No counterpart in the
+ * (bounded waits, reported by paliwa_gb_batch_status); it is the
+ * planner's default for 16-point wide chunks and an autotuner choice for
+ * the other wide classes. 0 keeps every such stage on the wide kernel's
+ * per-thread copies. Results are the same bits either way. Re-plans both
+ * directions after synchronizing the device. No counterpart in the
  * reference. */
 int paliwa_gb_batch_use_tma(paliwa_gb_batch *batch, int enable);
 /* ctas > 0 caps every launch of the batch at that many CTAs per SM (the
@@ -319,7 +320,8 @@ int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,
  * (bit 0 last axis, bit 1 sub-lattice of a long pencil, bits 2-7 log2 of the
  * pencil length, bits 8-11 log2 of the inner extent in bytes, capped at 8),
  * the kernels that apply (bit c for c = 0 staged with 16-point chunks,
- * 1 direct, 2 wide, 3 tile, 4 staged with 32-point chunks) and the chosen
+ * 1 direct, 2 wide, 3 tile, 4 staged with 32-point chunks, 5 the TMA wide
+ * kernel) and the chosen
  * one. Call with capacity 0 to get *nclasses first. */
 int paliwa_gb_batch_tuning(const paliwa_gb_batch *batch, int forward,
                            int capacity, int *nclasses, int32_t *classes,

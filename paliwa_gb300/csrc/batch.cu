@@ -79,8 +79,7 @@ struct Direction {
   // Slab launches where they apply (the batch's setting); the autotuner
   // clears it when the direction runs faster axis by axis.
   bool slabs = true;
-  // TMA wide launches for the strided wide stages (the batch's setting);
-  // the autotuner may clear it per direction.
+  // TMA wide launches for the stages planned on them (the batch's setting).
   bool tma = true;
   // Classes of the plan's periodic stages: applicable kernels (bits), the
   // default choice of the first stage seen, and the points they store.
@@ -424,7 +423,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
           if (k < stages[i].size()) {
             Stage const &st = stages[i][k];
             int code = st.R;
-            if (tma && twide_code(st.R) &&
+            if (tma && st.tma && twide_code(st.R) &&
                 canonical_shifts(st.job, (ws & 1) != 0))
               code = kTWide + (st.R - kWide);
             by_r[code].push_back(&st);
@@ -1140,21 +1139,6 @@ int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,
           ++nchanged;
         } else {
           dr.slabs = !dr.slabs;
-          replan(*batch, which);
-        }
-      }
-      // TMA wide launches against the wide kernel's own copies.
-      bool has_twide = false;
-      for (auto const &L : dr.launches) has_twide |= L.R > kTWide;
-      if (batch->use_tma && (has_twide || !dr.tma)) {
-        dr.tma = !dr.tma;
-        replan(*batch, which);
-        float const t = time_direction(*batch, which, reps, s);
-        if (t < best * 0.99f) {
-          best = t;
-          ++nchanged;
-        } else {
-          dr.tma = !dr.tma;
           replan(*batch, which);
         }
       }

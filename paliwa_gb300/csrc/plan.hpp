@@ -83,6 +83,8 @@ struct Stage {
   int tclass = 0;
   unsigned kernels = 0;
   int dflt = 0;
+  // A wide stage that a batch runs on the TMA wide kernel.
+  bool tma = false;
 };
 
 constexpr int kWindowLog2 = 12;   // points per column per CTA round (4096)
@@ -101,7 +103,10 @@ enum KernelChoice {
   kChooseWide = 2,
   kChooseTile = 3,
   kChooseStaged32 = 4,  // staged, 32 points per thread
-  kChooseCount = 5
+  // the wide kernel's transform with TMA copies (batches of FP32c grids;
+  // elsewhere the wide kernel)
+  kChooseTmaWide = 5,
+  kChooseCount = 6
 };
 struct KernelSet {
   unsigned mask = 0;  // a bit per applicable KernelChoice

@@ -220,7 +220,7 @@ class Batch:
             ctypes.byref(n)))
         return n.value
 
-    KERNELS = ("staged", "direct", "wide", "tile", "staged32")
+    KERNELS = ("staged", "direct", "wide", "tile", "staged32", "twide")
 
     def tuning(self, forward=True):
         """[(class, {last, sub, log2_n, log2_inner_bytes}, applicable kernel

@@ -145,9 +145,10 @@ struct paliwa_gb_batch {
   // The grids as created (for re-planning).
   std::vector<int64_t> levels, lmin;
   std::vector<void *> grids;
-  // Shadow buffers of the windowed stages (grids with pencils longer than
-  // one CTA holds), reused by every axis of a group (a group's axes run in
-  // order); the groups, which run concurrently, have disjoint regions.
+  // Halo buffers of the windowed stages (grids with pencils longer than one
+  // CTA holds; a region of the grid's size per grid and axis), reused by
+  // every axis of a group (a group's axes run in order); the groups, which
+  // run concurrently, have disjoint regions.
   void *shadow = nullptr;
   size_t shadow_bytes = 0;
   // group[g]: the group of grid g; group_shadow[k]: byte offset of group

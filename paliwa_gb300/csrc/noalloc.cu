@@ -5,8 +5,9 @@
 // a solver's arena), where a driver allocation can fail or fragment that
 // memory, and time-step loops that cannot pay for allocator calls or for the
 // device synchronization that cudaFree implies. paliwa_gb_hierarchize needs
-// scratch only for grids with a pencil longer than 4096 points (the shadow
-// buffer of its windowed stages) and takes it from the stream-ordered
+// scratch only for grids with a pencil longer than 4096 points (the halo
+// buffer of its windowed stages, the grid's size) and takes it from the
+// stream-ordered
 // allocator. This variant takes it from one file-scope device array instead
 // and allocates nothing.
 #include <array>

@@ -128,7 +128,8 @@ void plan_axis(AxisView const &view, std::vector<int> const &shifts,
 // halo pass the points it copies.
 long long stage_points(Stage const &st);
 
-// True when planning `view` along `shifts` needs a shadow buffer.
+// True when planning `view` along `shifts` needs a halo buffer (the field
+// `shadow`: the grid's size and layout).
 inline bool needs_shadow(AxisView const &view, std::vector<int> const &shifts) {
   return !shifts.empty() && view.log2_n > kWindowLog2;
 }

@@ -7,9 +7,8 @@
 // device synchronization that cudaFree implies. paliwa_gb_hierarchize needs
 // scratch only for grids with a pencil longer than 4096 points (the halo
 // buffer of its windowed stages, the grid's size) and takes it from the
-// stream-ordered
-// allocator. This variant takes it from one file-scope device array instead
-// and allocates nothing.
+// stream-ordered allocator. This variant takes it from one file-scope device
+// array instead and allocates nothing.
 #include <array>
 #include <cstdint>
 #include <mutex>

@@ -326,6 +326,15 @@ int paliwa_gb_batch_autotune(paliwa_gb_batch *batch, void *stream, int reps,
 int paliwa_gb_batch_tuning(const paliwa_gb_batch *batch, int forward,
                            int capacity, int *nclasses, int32_t *classes,
                            int32_t *kernels, int32_t *choices);
+/* Sets the kernel of `nclasses` classes of one direction's plan (codes and
+ * kernel numbers as paliwa_gb_batch_tuning reports them) and re-plans that
+ * direction, e.g. to replay an earlier autotuner result without timing.
+ * PALIWA_GB_INVALID_ARGUMENT, with nothing changed, when a class has no
+ * stage in the batch or the kernel does not apply to it. Every kernel gives
+ * the same results. */
+int paliwa_gb_batch_set_tuning(paliwa_gb_batch *batch, int forward,
+                               int nclasses, const int32_t *classes,
+                               const int32_t *choices);
 void paliwa_gb_batch_destroy(paliwa_gb_batch *batch);
 
 /* ------------------------------------------------------------------------

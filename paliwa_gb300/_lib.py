@@ -79,6 +79,9 @@ SIGNATURES = {
     "paliwa_gb_batch_tuning": (
         _i, [_vp, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_int32),
              ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "paliwa_gb_batch_set_tuning": (
+        _i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_int32),
+             ctypes.POINTER(ctypes.c_int32)]),
     "paliwa_gb_batch_destroy": (None, [_vp]),
     "paliwa_gb_ct_create": (
         _i, [_i, _i, _pi64, _pd, _pi64, _i, ctypes.POINTER(_vp), _i,

@@ -1202,6 +1202,39 @@ int paliwa_gb_batch_tuning(const paliwa_gb_batch *batch, int forward,
   });
 }
 
+int paliwa_gb_batch_set_tuning(paliwa_gb_batch *batch, int forward,
+                               int nclasses, const int32_t *classes,
+                               const int32_t *choices) {
+  return guarded([&] {
+    if (batch == nullptr || nclasses < 0 ||
+        (nclasses > 0 && (classes == nullptr || choices == nullptr)))
+      throw StatusError(PALIWA_GB_INVALID_ARGUMENT, "null argument");
+    int const which = forward ? 0 : 1;
+    Direction &dr = batch->dir[which];
+    // Check every entry before changing anything.
+    for (int i = 0; i < nclasses; ++i) {
+      auto const it = dr.classes.find(classes[i]);
+      if (it == dr.classes.end())
+        throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                          "no stage of the batch is in tuning class " +
+                              std::to_string(classes[i]));
+      if (choices[i] < 0 || choices[i] >= kChooseCount ||
+          !((it->second.kernels >> choices[i]) & 1u))
+        throw StatusError(PALIWA_GB_INVALID_ARGUMENT,
+                          "kernel " + std::to_string(choices[i]) +
+                              " does not apply to tuning class " +
+                              std::to_string(classes[i]));
+    }
+    for (int i = 0; i < nclasses; ++i) {
+      if (choices[i] == dr.classes.at(classes[i]).dflt)
+        dr.tuning.choice.erase(classes[i]);
+      else
+        dr.tuning.choice[classes[i]] = choices[i];
+    }
+    replan(*batch, which);
+  });
+}
+
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,
                             int64_t *bytes, int32_t *kernels) {

@@ -14,10 +14,21 @@
 // mbarrier with a bounded wait. After the transform the threads write their
 // rows back into the same place and one thread stores the boxes with bulk
 // tensor stores. Columns past the end of the grid are read as zeros and not
-// stored (the tensor map's bounds). Each CTA keeps S tiles in flight: the
-// copies are asynchronous and issued by one thread, which removes the
-// per-thread copy instructions that throttled the wide kernel's memory
-// pipeline (measured on a copy-only build: MIO throttle of 10 per issue).
+// stored (the tensor map's bounds). The copies are asynchronous and issued
+// by one thread, which removes the per-thread copy instructions that
+// throttled the wide kernel's memory pipeline (measured on a copy-only
+// build: MIO throttle of 10 per issue).
+//
+// The CTA is warp-specialised: NT transform threads (eight warps) and one
+// producer warp, of which one lane issues every copy. S tile buffers cycle
+// through two mbarriers each: `full` (the tile's loads have landed; the
+// producer arrives with the byte count) and `empty` (all NT transform
+// threads have written the tile back). The producer stores a tile once it is
+// empty, waits until that store has read the buffer, and loads the tile S
+// later into it; the transform warps never meet at a CTA barrier and never
+// wait for a store (a version with one CTA barrier per tile and the copies
+// issued by thread 0 between tiles stalled on the barrier more than on
+// anything else).
 //
 // The maps live in global memory, written by the host before the launch;
 // they cover only this GPU's grid memory (no multicast).
@@ -31,7 +42,8 @@
 
 namespace pgb {
 
-constexpr int kTWideThreads = 256;
+constexpr int kTWideThreads = 256;               // transform threads
+constexpr int kTWideBlock = kTWideThreads + 32;  // + the producer warp
 
 struct TWideJob {
   long long tile_begin;  // first tile of this job in the launch
@@ -81,30 +93,40 @@ __device__ __forceinline__ void fence_tensormap(void const *map) {
 
 // A tile is kUnits units of Ct * n * 4 = (2 NT / G) * (G R) * 4 bytes
 // (16 KB tiles for chunks of up to 8 points: per-tile synchronisation
-// dominated 8 KB ones). kStages tiles per CTA: one transformed, kLook
-// loading ahead, and kDefer whose stores may still be reading shared memory
-// when a buffer is reloaded (so the reload does not wait for the store just
-// issued).
+// dominated 8 KB ones); kStages tile buffers per CTA.
 template <int R> struct TWideShape {
   static constexpr int kUnits = R >= 8 ? 1 : 8 / R;
   static constexpr int kUnitBytes = 8 * kTWideThreads * R;
   static constexpr int kTileBytes = kUnits * kUnitBytes;
   static constexpr int kStages = R >= 16 ? 3 : 4;
-  static constexpr int kDefer = R >= 16 ? 0 : 1;
-  static constexpr int kLook = kStages - 1 - kDefer;
   static constexpr size_t kSmemBytes =
       size_t(kStages) * kTileBytes + 128;  // + 128-byte alignment slack
 };
 
-__device__ __forceinline__ void bulk_wait_read_1() {
-  asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
-}
 template <int R> constexpr size_t twide_smem_bytes() {
   return TWideShape<R>::kSmemBytes;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+// Waits for phase `parity` of `bar` for about a second of clock, or until
+// *abort is set; false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
+                                                  unsigned parity,
+                                                  int const volatile *abort) {
+  long long const t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if ((abort != nullptr && *abort) || clock64() - t0 > (1LL << 31))
+      return false;
+  return true;
+}
+
 template <class A, int R, class Sched>
-__global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
+__global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     twide_kernel(__grid_constant__ const TWideParams p) {
   using V = typename A::V;
   using W = typename A::Store;
@@ -114,16 +136,16 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
   constexpr int TILE = TWideShape<R>::kTileBytes;
   constexpr int U = TWideShape<R>::kUnits;
   constexpr int UNIT = TWideShape<R>::kUnitBytes;
-  constexpr int LOOK = TWideShape<R>::kLook;
-  constexpr int DEFER = TWideShape<R>::kDefer;
   constexpr int LOG2R = Log2<R>::value;
   constexpr int LOG2NT = Log2<NT>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned const base_addr = smem_u32(smem_raw);
   unsigned char *const tiles =
       smem_raw + ((128 - (base_addr & 127)) & 127);  // 128-byte aligned
-  __shared__ uint64_t full[S];
+  __shared__ uint64_t full[S], empty[S];
   __shared__ TWideJob sjob[S];
+  __shared__ int abort_flag;  // set when a bounded wait gave up
+  int volatile *const abort = &abort_flag;
 
   int const t = threadIdx.x;
   int const lane = t & 31;
@@ -133,10 +155,14 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
   long long const ntiles = (p.total_tiles - first + step - 1) / step;
 
   if (t == 0) {
-    for (int b = 0; b < S; ++b) mbar_init(&full[b], 1);
+    for (int b = 0; b < S; ++b) {
+      mbar_init(&full[b], 1);
+      mbar_init(&empty[b], NT);
+    }
+    *abort = 0;
     fence_mbar_init();
   }
-  __syncthreads();
+  __syncthreads();  // the CTA's only barrier
 
   // Unit u of tile `tile` of `job`: its first column's (inner, outer)
   // coordinates.
@@ -162,7 +188,7 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
     return 4 << (job.log2_bx + job.log2_n + job.log2_sx);
   };
 
-  // Thread 0 issues every copy; it keeps the last map it fenced.
+  // The producer lane issues every copy; it keeps the last map it fenced.
   int fenced = -1;
   auto issue_load = [&](long long k) {
     int const b = static_cast<int>(k % S);
@@ -206,86 +232,93 @@ __global__ void __launch_bounds__(kTWideThreads, R >= 16 ? 2 : R == 8 ? 3 : 4)
     bulk_commit();
   };
 
-  long long issued = 0;
-  if (t == 0)
-    for (; issued < LOOK && issued < ntiles; ++issued) issue_load(issued);
-
-  long long k = 0;
-  bool failed = false;
-  for (; k < ntiles; ++k) {
-    int const b = static_cast<int>(k % S);
-    if (t == 0 && issued < ntiles) {
-      // The buffer of tile k + LOOK held tile k + LOOK - S = k - 1 - DEFER:
-      // its stores (all but the DEFER most recent store groups) must have
-      // read it.
-      if constexpr (DEFER == 0)
-        bulk_wait_read_all();
-      else
-        bulk_wait_read_1();
-      issue_load(issued);
-      ++issued;
+  if (t >= NT) {
+    // Producer warp: lane 0 alone.
+    if (t != NT) return;
+    long long issued = 0;
+    for (; issued < S && issued < ntiles; ++issued) issue_load(issued);
+    bool failed = false;
+    for (long long k = 0; k < ntiles; ++k) {
+      int const b = static_cast<int>(k % S);
+      if (!mbar_wait_bounded(&empty[b], static_cast<unsigned>((k / S) & 1),
+                             abort)) {
+        failed = true;
+        break;
+      }
+      issue_store(k);
+      if (issued < ntiles) {  // issued == k + S: the next tile for buffer b
+        bulk_wait_read_all();  // the store just issued has read buffer b
+        issue_load(issued);
+        ++issued;
+      }
     }
-    // Bounded wait for tile k (about a second of clock), then a vote so
-    // that every thread leaves together if it gave up.
-    unsigned const parity = static_cast<unsigned>((k / S) & 1);
-    bool done = false;
-    long long const t0 = clock64();
-    while (!(done = mbar_try_wait(&full[b], parity)))
-      if (clock64() - t0 > (1LL << 31)) break;
-    if (!__syncthreads_and(done)) {
-      failed = true;
+    if (failed) {
+      atomicExch(p.error, 1u);
+      *abort = 1;
+      // Wait (bounded) for the last load issued into each buffer, so that
+      // no copy is in flight when the CTA's shared memory goes away.
+      for (long long q = issued > S ? issued - S : 0; q < issued; ++q)
+        mbar_wait_bounded(&full[q % S], static_cast<unsigned>((q / S) & 1),
+                          nullptr);
+    }
+    bulk_wait_all();
+    return;
+  }
+
+  // Transform threads.
+  for (long long k = 0; k < ntiles; ++k) {
+    int const b = static_cast<int>(k % S);
+    bool const ok = mbar_wait_bounded(
+        &full[b], static_cast<unsigned>((k / S) & 1), abort);
+    // A warp leaves as a whole (its lanes exchange by shuffles).
+    if (!__all_sync(0xffffffffu, ok)) {
+      if (lane == 0) {
+        atomicExch(p.error, 1u);
+        *abort = 1;
+      }
       break;
     }
     TWideJob const &job = sjob[b];
     // Thread = (chunk c, column pair g): the chunks of a column pair are
     // lanes W = 32 / G apart, the W column pairs of one chunk consecutive.
     int const log2G = job.log2_n - LOG2R;
-    int const log2W = 5 - log2G;
-    int const c = lane >> log2W;
-    int const g = ((t >> 5) << log2W) | (lane & ((1 << log2W) - 1));
-    int const col = 2 * g;
-    int const log2bs = job.log2_bx + job.log2_sx;
-    int const xb = col >> log2bs;
-    int const rem = col & ((1 << log2bs) - 1);
-    int const s = rem >> job.log2_bx;
-    int const bcol = rem & ((1 << job.log2_bx) - 1);
-    // float index of row c R of the thread's columns; rows are Bx apart
-    int const idx0 = (xb << (log2bs + job.log2_n)) +
-                     ((((s << job.log2_n) + (c << LOG2R)) << job.log2_bx) +
-                      bcol);
-    for (int u = 0; u < U; ++u) {
-      float *const tf =
-          reinterpret_cast<float *>(tiles + b * TILE + u * UNIT);
-      V v[R];
+    // The planner gives at most 4 chunks per pencil; more than 32 would take
+    // the exchange paths that need a CTA barrier, which this kernel has not.
+    if (static_cast<unsigned>(log2G) <= 5u) {
+      int const log2W = 5 - log2G;
+      int const c = lane >> log2W;
+      int const g = ((t >> 5) << log2W) | (lane & ((1 << log2W) - 1));
+      int const col = 2 * g;
+      int const log2bs = job.log2_bx + job.log2_sx;
+      int const xb = col >> log2bs;
+      int const rem = col & ((1 << log2bs) - 1);
+      int const s = rem >> job.log2_bx;
+      int const bcol = rem & ((1 << job.log2_bx) - 1);
+      // float index of row c R of the thread's columns; rows are Bx apart
+      int const idx0 = (xb << (log2bs + job.log2_n)) +
+                       ((((s << job.log2_n) + (c << LOG2R)) << job.log2_bx) +
+                        bcol);
+      for (int u = 0; u < U; ++u) {
+        float *const tf =
+            reinterpret_cast<float *>(tiles + b * TILE + u * UNIT);
+        V v[R];
 #pragma unroll
-      for (int j = 0; j < R; ++j)
-        v[j] = A::load(
-            *reinterpret_cast<W const *>(tf + idx0 + (j << job.log2_bx)));
-      RoundCtx<A, NT> ctx(t, c, 1 << log2G, log2G, lane, 1, nullptr, nullptr,
-                          log2W);
-      Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
+        for (int j = 0; j < R; ++j)
+          v[j] = A::load(
+              *reinterpret_cast<W const *>(tf + idx0 + (j << job.log2_bx)));
+        RoundCtx<A, NT> ctx(t, c, 1 << log2G, log2G, lane, 1, nullptr,
+                            nullptr, log2W);
+        Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
 #pragma unroll
-      for (int j = 0; j < R; ++j)
-        *reinterpret_cast<W *>(tf + idx0 + (j << job.log2_bx)) =
-            A::store(v[j]);
-    }
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (t == 0) issue_store(k);
-  }
-  if (t == 0) {
-    if (failed) {
-      atomicExch(p.error, 1u);
-      // Wait (bounded) for the loads still in flight before the CTA's
-      // shared memory goes away.
-      for (long long q = k; q < issued; ++q) {
-        unsigned const par = static_cast<unsigned>((q / S) & 1);
-        long long const t0 = clock64();
-        while (!mbar_try_wait(&full[q % S], par))
-          if (clock64() - t0 > (1LL << 31)) break;
+        for (int j = 0; j < R; ++j)
+          *reinterpret_cast<W *>(tf + idx0 + (j << job.log2_bx)) =
+              A::store(v[j]);
       }
+    } else if (lane == 0) {
+      atomicExch(p.error, 1u);
     }
-    bulk_wait_all();
+    fence_proxy_async_smem();  // the writes above, before the tile's store
+    mbar_arrive(&empty[b]);
   }
 }
 

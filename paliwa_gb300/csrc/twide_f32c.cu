@@ -24,7 +24,7 @@ void launch_twide_r(TWideParams const &p, cudaStream_t s) {
                "cudaFuncSetAttribute(twide)");
     int n = 0;
     cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &n, kernel, kTWideThreads, smem),
+                   &n, kernel, kTWideBlock, smem),
                "occupancy query (twide)");
     sms = device_sms();
     per_sm = n < 1 ? 1 : n;
@@ -32,7 +32,7 @@ void launch_twide_r(TWideParams const &p, cudaStream_t s) {
   long long const resident =
       static_cast<long long>(capped_per_sm(per_sm, p.ctas_per_sm)) * sms;
   long long const blocks = std::min(p.total_tiles, resident);
-  kernel<<<static_cast<unsigned>(blocks), kTWideThreads, smem, s>>>(p);
+  kernel<<<static_cast<unsigned>(blocks), kTWideBlock, smem, s>>>(p);
   cuda_check(cudaGetLastError(), "twide kernel launch");
 }
 

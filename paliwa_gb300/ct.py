@@ -242,6 +242,20 @@ class Batch:
             out.append((c, desc, names, self.KERNELS[x]))
         return out
 
+    def set_tuning(self, choices, forward=True):
+        """Set the kernel of classes of one direction's plan: `choices` maps
+        class codes (as tuning() reports them) to kernel names or numbers.
+        Raises ValueError, changing nothing, for a class the plan lacks or a
+        kernel that does not apply to it."""
+        items = list(choices.items())
+        cl = (ctypes.c_int32 * max(1, len(items)))()
+        ch = (ctypes.c_int32 * max(1, len(items)))()
+        for i, (c, k) in enumerate(items):
+            cl[i] = int(c)
+            ch[i] = self.KERNELS.index(k) if isinstance(k, str) else int(k)
+        _lib.check(self._lib.paliwa_gb_batch_set_tuning(
+            self._h, int(forward), len(items), cl, ch))
+
     def close(self):
         if self._h:
             self._lib.paliwa_gb_batch_destroy(self._h)

@@ -486,3 +486,61 @@ def test_tma_wide_kernel_gives_the_wide_kernels_bits():
             b.close()
         assert torch.equal(out[0][0], out[1][0]), wavelet
         assert torch.equal(out[0][1], out[1][1]), wavelet
+
+
+def test_every_tma_wide_class_gives_the_wide_kernels_bits():
+    """Chunks of 2, 4, 8 and 16 points: every class of stages that the TMA
+    wide kernel applies to, set to it through set_tuning, gives the bits of
+    the same classes set to the per-thread-copy wide kernel, forward and
+    inverse, for every wavelet. A kernel that does not apply, or a class the
+    plan lacks, is refused with nothing changed."""
+    import torch
+    levels = [(6, 1, 3), (5, 2, 2), (4, 6, 1), (3, 3, 5), (6, 6, 2), (2, 5, 7),
+              (1, 4, 9), (6, 2, 1), (2, 2, 2), (5, 5, 5), (4, 1, 10),
+              (3, 2, 8), (2, 3, 6)]
+    lmin, lmax = (1, 1, 1), (14, 14, 14)
+    rng = np.random.default_rng(78)
+    host = [rng.uniform(-1, 1, 1 << sum(l)).astype(np.float32)
+            for l in levels]
+    seen = set()
+    for wavelet in ("hat", "biorthogonal", "fullweighting"):
+        out = []
+        for kernel in ("twide", "wide"):
+            buf, gs = pct.packed_grids(levels, torch.float32)
+            # no slabs: the small grids' axes would go to the slab kernel
+            b = pct.Batch(gs, levels, lmin, lmax, wavelet, compensated=True,
+                          slabs=False)
+            for forward in (True, False):
+                cls = {c: kernel for c, _, names, _ in b.tuning(forward)
+                       if "twide" in names}
+                assert cls, "no class of the scheme takes the TMA wide kernel"
+                b.set_tuning(cls, forward)
+                assert all(ch == kernel for c, _, _, ch in b.tuning(forward)
+                           if c in cls)
+                if kernel == "twide":
+                    seen.update(d["log2_n"] for c, d, _, _ in
+                                b.tuning(forward) if c in cls)
+            s = torch.cuda.Stream()
+            kernels = b.profile(True, stream=s)[2]
+            assert any(k > pct.TWIDE_KERNEL for k in kernels) == \
+                (kernel == "twide")
+            for g, h in zip(gs, host):
+                g.copy_(torch.from_numpy(h))
+            b.hierarchize(s)
+            s.synchronize()
+            fwd = buf.clone()
+            b.dehierarchize(s)
+            s.synchronize()
+            b.status()
+            out.append((fwd, buf.clone()))
+            if kernel == "wide":
+                c0 = b.tuning(True)[0][0]
+                with pytest.raises(ValueError):
+                    b.set_tuning({c0: "twide", 1 << 20: "wide"})
+                with pytest.raises(ValueError):
+                    b.set_tuning({c0: 99})
+            b.close()
+        assert torch.equal(out[0][0], out[1][0]), wavelet
+        assert torch.equal(out[0][1], out[1][1]), wavelet
+    # pencils of 4 to 64 points (axes at level 1 = lmin have nothing to do)
+    assert {2, 3, 4, 5, 6} <= seen, seen

@@ -255,17 +255,18 @@ int paliwa_gb_batch_set_groups(paliwa_gb_batch *batch, int ngroups);
  * directions after synchronizing the device. No counterpart in the
  * reference. */
 int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable);
-/* enable != 0 (default): FP32-compensated strided stages that the wide
- * kernel takes (pencils of up to 64 points, inner extent of 4 or more
- * columns, 16-byte aligned grids) run on the TMA wide kernel: the same
- * register transform, with each tile of columns moved between HBM and
- * shared memory by bulk tensor copies over a tensor map of the grid's axis
- * (bounded waits, reported by paliwa_gb_batch_status); it is the
- * planner's default for 16-point wide chunks and an autotuner choice for
- * the other wide classes. 0 keeps every such stage on the wide kernel's
- * per-thread copies. Results are the same bits either way. Re-plans both
- * directions after synchronizing the device. No counterpart in the
- * reference. */
+/* enable != 0 (default): FP32-compensated strided stages of up to 16
+ * chunks per pencil (the wide kernel's pencils of up to 64 points and the
+ * tile kernel's of 128 and 256; inner extent of 4 or more columns, 16-byte
+ * aligned grids) may run on the TMA wide kernel: the wide kernel's register
+ * transform, with each tile of columns moved between HBM and shared memory
+ * by bulk tensor copies over a tensor map of the grid's axis (bounded
+ * waits, reported by paliwa_gb_batch_status). It is the planner's default
+ * for wide chunks of 8 and 16 points and for pencils of 128 and 256 points,
+ * and an autotuner choice for the others. 0 keeps every such stage on the
+ * wide or tile kernel's per-thread copies. Results are the same bits either
+ * way. Re-plans both directions after synchronizing the device. No
+ * counterpart in the reference. */
 int paliwa_gb_batch_use_tma(paliwa_gb_batch *batch, int enable);
 /* ctas > 0 caps every launch of the batch at that many CTAs per SM (the
  * kernels are persistent: by default a launch takes every slot that fits),

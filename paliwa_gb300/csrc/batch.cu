@@ -286,26 +286,34 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return encode;
 }
 
-// Stage codes of the strided wide kernel that the TMA wide kernel takes.
-bool twide_code(int R) {
-  return R == kWide + 2 || R == kWide + 4 || R == kWide + 8 ||
-         R == kWide + 16;
+// Chunk size of the TMA wide launch that may take a stage (the stage's own
+// kernel otherwise): strided wide stages (chunks of 2-16 points, up to 4 per
+// pencil) and tile stages of 8 or 16 chunks of 16 points; 0 for the rest.
+int twide_chunk(Stage const &st) {
+  int const R = st.R;
+  if (R == kWide + 2 || R == kWide + 4 || R == kWide + 8 || R == kWide + 16)
+    return R - kWide;
+  if ((R == kTile + 16 || R == kTileLong + 16) && st.job.log2_n >= 7 &&
+      st.job.log2_n <= 8)
+    return 16;
+  return 0;
 }
 
-// The TMA wide job and tensor map of a strided wide stage (FP32c, float
-// storage): the 3D view [outer][n][inner] of the stage's pencils with the
-// axis' strides, boxes {Bx, n, Sx} covering one tile of Ct = 2 NT / G
-// columns. False when the stage does not qualify (alignment, inner extent
-// under 4 columns, 2^30 tiles or more, or the encoder refuses the map).
-bool twide_job(Stage const &st, TWideJob &job, CUtensorMap &map,
+// The TMA wide job and tensor map of a strided stage (FP32c, float storage)
+// with chunks of r points: the 3D view [outer][n][inner] of the stage's
+// pencils with the axis' strides, boxes {Bx, n, Sx} covering one tile of
+// Ct = 2 NT / G columns. False when the stage does not qualify
+// (alignment, inner extent under 4 columns, more than 16 chunks, 2^30 tiles
+// or more, or the encoder refuses the map).
+bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
                long long &tiles) {
   auto encode = tensor_map_encoder();
   LiftJob const &lj = st.job;
-  int const r = st.R - kWide;
   int const log2r = 31 - __builtin_clz(static_cast<unsigned>(r));
   int const log2G = lj.log2_n - log2r;
   if (encode == nullptr || lj.periodic != 1 || lj.base % 16 != 0 ||
-      lj.log2_inner < 2 || log2G < 0 || log2G > 2 || lj.log2_n > 6)
+      lj.log2_inner < 2 || log2G < 0 || log2G > 4 || lj.log2_n > 8 ||
+      (log2G > 2 && r != 16))
     return false;
   int const log2ct = Log2<kTWideThreads>::value + 1 - log2G;
   // Units per tile: TWideShape<R>::kUnits (16 KB tiles for chunks of up to
@@ -424,9 +432,10 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
           if (k < stages[i].size()) {
             Stage const &st = stages[i][k];
             int code = st.R;
-            if (tma && st.tma && twide_code(st.R) &&
+            int const r = twide_chunk(st);
+            if (tma && st.tma && r > 0 &&
                 canonical_shifts(st.job, (ws & 1) != 0))
-              code = kTWide + (st.R - kWide);
+              code = kTWide + r;
             by_r[code].push_back(&st);
           }
         for (auto const &[R, list] : by_r) {
@@ -437,13 +446,14 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
             L.sched = ws;
             L.job_first = all_twide.size();
             L.tile_first = twide_tiles.size();
-            std::vector<Stage const *> rest;  // stages that do not qualify
+            // Stages that do not qualify, by their own kernel.
+            std::map<int, std::vector<Stage const *>> rest;
             for (Stage const *st : list) {
               TWideJob job;
               CUtensorMap map;
               long long tiles = 0;
-              if (!twide_job(*st, job, map, tiles)) {
-                rest.push_back(st);
+              if (!twide_job(*st, R - kTWide, job, map, tiles)) {
+                rest[st->R].push_back(st);
                 continue;
               }
               job.tile_begin = L.tiles;
@@ -456,22 +466,22 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
               ++L.njobs;
             }
             if (L.njobs > 0) dr.launches.push_back(L);
-            if (rest.empty()) continue;
-            // The rest on the wide kernel.
-            Launch W;
-            W.group = grp;
-            W.R = kWide + (R - kTWide);
-            W.sched = ws;
-            W.job_first = all_jobs.size();
-            W.njobs = static_cast<int>(rest.size());
-            for (Stage const *st : rest) {
-              LiftJob job = st->job;
-              job.tile_begin = W.tiles;
-              W.tiles += st->tiles;
-              W.points += stage_points(*st);
-              all_jobs.push_back(job);
+            for (auto const &[rR, rlist] : rest) {
+              Launch W;
+              W.group = grp;
+              W.R = rR;
+              W.sched = ws;
+              W.job_first = all_jobs.size();
+              W.njobs = static_cast<int>(rlist.size());
+              for (Stage const *st : rlist) {
+                LiftJob job = st->job;
+                job.tile_begin = W.tiles;
+                W.tiles += st->tiles;
+                W.points += stage_points(*st);
+                all_jobs.push_back(job);
+              }
+              dr.launches.push_back(W);
             }
-            dr.launches.push_back(W);
             continue;
           }
           Launch L;

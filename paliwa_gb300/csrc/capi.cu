@@ -201,16 +201,20 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
       ((!last && wide_chunk(v.log2_n) > 0 && v.log2_inner >= v.log2_row) ||
        (last && log2G <= 5 && v.columns >= (1LL << v.log2_row))))
     k.mask |= 1 << kChooseWide;
-  // The TMA wide kernel: FP32c strided wide stages, 16-byte aligned, inner
-  // extents of 4 or more columns, pencils of up to 4 chunks.
-  if (k.has(kChooseWide) && !last && v.wide_last && v.log2_inner >= 2 &&
-      v.base % 16 == 0 && v.log2_n - (31 - __builtin_clz(static_cast<unsigned>(
-                                          wide_chunk(v.log2_n)))) <= 2)
-    k.mask |= 1 << kChooseTmaWide;
   if (aligned && !last && R == 16 && log2G >= 3 && log2G <= 8 &&
       v.log2_inner + v.log2_es >=
           tile_piece_log2(log2G, v.log2_row + v.log2_es))
     k.mask |= 1 << kChooseTile;
+  // The TMA wide kernel: FP32c strided stages, 16-byte aligned, inner
+  // extents of 4 or more columns; wide stages of up to 4 chunks, and tile
+  // stages of 8 or 16 chunks of 16 points (pencils of 128 and 256 points).
+  if (!last && v.wide_last && v.log2_inner >= 2 && v.base % 16 == 0 &&
+      v.columns < (1LL << 30) &&
+      ((k.has(kChooseWide) &&
+        v.log2_n - (31 - __builtin_clz(static_cast<unsigned>(
+                             wide_chunk(v.log2_n)))) <= 2) ||
+       (k.has(kChooseTile) && log2G >= 3 && log2G <= 4)))
+    k.mask |= 1 << kChooseTmaWide;
   // Default: the wide kernel for strided pencils (and FP32c last-axis
   // pencils: measured on 2^26-point grids, 3.0-4.5 TB/s against 2.8-4.1 on
   // the direct kernel), then the tile kernel up to the length where it was
@@ -220,9 +224,14 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   // 8-byte copy pieces, and beyond 32 chunks the batch ran slower than on
   // the staged kernel); then the direct kernel, then the staged one.
   int const tile_log2G_max = v.wide_last ? 4 : v.log2_es == 3 ? 5 : 8;
-  // (The TMA wide kernel is the default for 16-point wide chunks, where it
-  // measured faster per launch on the 4D CT batch: 3.96 against 3.16 TB/s.)
-  if (k.has(kChooseTmaWide) && wide_chunk(v.log2_n) == 16)
+  // (The TMA wide kernel is the default for wide chunks of 8 and 16 points
+  // and for pencils of 8 or 16 chunks, where it measured faster per launch
+  // on the 4D CT batch: 4.73 against 4.01 TB/s at 8 points, 4.73 against
+  // 3.16 at 16, about 3.7 against 2.29 on the tile kernel's pencils of 128
+  // and 256 points; at 4 points the wide kernel is faster, 5.26 against
+  // 4.39-4.55 TB/s.)
+  if (k.has(kChooseTmaWide) &&
+      (!k.has(kChooseWide) || wide_chunk(v.log2_n) >= 8))
     k.dflt = kChooseTmaWide;
   else if (k.has(kChooseWide) && (!last || v.wide_last))
     k.dflt = kChooseWide;
@@ -275,9 +284,20 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
       if (it != tuning->choice.end() && ks.has(it->second))
         choice = it->second;
     }
+    auto tile_stage = [&] {
+      st.R = (log2G <= 5 ? kTile : kTileLong) + 16;
+      st.job.col_tiles =
+          ceil_div(v.columns >> v.log2_row, kThreads >> log2G);
+    };
     switch (choice) {
     case kChooseTmaWide:
+      // Marked for the TMA wide kernel (batches); elsewhere, and for the
+      // grids that do not qualify, the kernel it stands in for.
       st.tma = true;
+      if (!ks.has(kChooseWide)) {
+        tile_stage();
+        break;
+      }
       [[fallthrough]];
     case kChooseWide:
       if (last) {
@@ -289,9 +309,7 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
       }
       break;
     case kChooseTile:
-      st.R = (log2G <= 5 ? kTile : kTileLong) + 16;
-      st.job.col_tiles =
-          ceil_div(v.columns >> v.log2_row, kThreads >> log2G);
+      tile_stage();
       break;
     case kChooseDirect:
       st.R = -R;

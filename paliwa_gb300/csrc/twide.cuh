@@ -1,8 +1,8 @@
 // TMA wide kernel: the wide kernel's register transform (rows of two
 // adjacent columns as double-float f32x2 pairs, chunks of one pencil in
 // lanes 32 / G apart, shuffles only) for strided axes with pencils of up to
-// 64 points, with the data moved by the tensor memory accelerator instead
-// of per-thread copies.
+// 256 points (G <= 16 chunks), with the data moved by the tensor memory
+// accelerator instead of per-thread copies.
 //
 // A tile is one unit of the wide kernel: NT threads x R rows x 2 columns =
 // Ct = 2 NT / G consecutive columns (column = (outer index, inner index)) of
@@ -11,9 +11,13 @@
 // a tile is 1 or 2 boxes {Bx columns of one outer index, n rows, Sx outer
 // indices} (Bx = min(inner, Ct, 256), Sx = Ct / inner when inner < Ct),
 // loaded into shared memory as [box][outer][row][column], completion on an
-// mbarrier with a bounded wait. After the transform the threads write their
-// rows back into the same place and one thread stores the boxes with bulk
-// tensor stores. Columns past the end of the grid are read as zeros and not
+// mbarrier with a bounded wait. Every box starts on a 128-byte boundary of
+// shared memory, as bulk tensor copies require; so the G chunks of a warp,
+// R rows apart, read the same banks (a G-way conflict on 8 or more chunks:
+// a pad after one box per chunk would remove it, but would move the boxes
+// off the 128-byte boundaries). After the transform the threads write
+// their rows back into the same place and one thread stores the boxes with
+// bulk tensor stores. Columns past the end of the grid are read as zeros and not
 // stored (the tensor map's bounds). The copies are asynchronous and issued
 // by one thread, which removes the per-thread copy instructions that
 // throttled the wide kernel's memory pipeline (measured on a copy-only
@@ -282,8 +286,9 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     // Thread = (chunk c, column pair g): the chunks of a column pair are
     // lanes W = 32 / G apart, the W column pairs of one chunk consecutive.
     int const log2G = job.log2_n - LOG2R;
-    // The planner gives at most 4 chunks per pencil; more than 32 would take
-    // the exchange paths that need a CTA barrier, which this kernel has not.
+    // The planner gives at most 16 chunks per pencil; more than 32 would
+    // take the exchange paths that need a CTA barrier, which this kernel
+    // has not.
     if (static_cast<unsigned>(log2G) <= 5u) {
       int const log2W = 5 - log2G;
       int const c = lane >> log2W;

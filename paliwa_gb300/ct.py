@@ -151,9 +151,10 @@ class Batch:
         _lib.check(self._lib.paliwa_gb_batch_use_slabs(self._h, int(enable)))
 
     def use_tma(self, enable):
-        """Run the FP32c strided stages of the wide kernel on the TMA wide
-        kernel (default), or on the wide kernel's per-thread copies (the
-        same bits). Synchronizes the device."""
+        """Run FP32c strided stages of up to 16 chunks per pencil on the TMA
+        wide kernel where the plan chose it (default), or on the wide and
+        tile kernels' per-thread copies (the same bits). Synchronizes the
+        device."""
         _lib.check(self._lib.paliwa_gb_batch_use_tma(self._h, int(enable)))
 
     def set_ctas_per_sm(self, ctas):

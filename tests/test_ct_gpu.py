@@ -489,15 +489,17 @@ def test_tma_wide_kernel_gives_the_wide_kernels_bits():
 
 
 def test_every_tma_wide_class_gives_the_wide_kernels_bits():
-    """Chunks of 2, 4, 8 and 16 points: every class of stages that the TMA
-    wide kernel applies to, set to it through set_tuning, gives the bits of
-    the same classes set to the per-thread-copy wide kernel, forward and
-    inverse, for every wavelet. A kernel that does not apply, or a class the
-    plan lacks, is refused with nothing changed."""
+    """Chunks of 2, 4, 8 and 16 points, up to 16 chunks per pencil: every
+    class of stages that the TMA wide kernel applies to, set to it through
+    set_tuning, gives the bits of the same classes set to the per-thread-copy
+    wide kernel (or, for pencils of 128 and 256 points, the tile kernel),
+    forward and inverse, for every wavelet. A kernel that does not apply, or
+    a class the plan lacks, is refused with nothing changed."""
     import torch
     levels = [(6, 1, 3), (5, 2, 2), (4, 6, 1), (3, 3, 5), (6, 6, 2), (2, 5, 7),
               (1, 4, 9), (6, 2, 1), (2, 2, 2), (5, 5, 5), (4, 1, 10),
-              (3, 2, 8), (2, 3, 6)]
+              (3, 2, 8), (2, 3, 6), (7, 4, 3), (8, 5, 1), (2, 8, 4),
+              (7, 2, 2), (13, 2, 1)]
     lmin, lmax = (1, 1, 1), (14, 14, 14)
     rng = np.random.default_rng(78)
     host = [rng.uniform(-1, 1, 1 << sum(l)).astype(np.float32)
@@ -505,17 +507,21 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
     seen = set()
     for wavelet in ("hat", "biorthogonal", "fullweighting"):
         out = []
-        for kernel in ("twide", "wide"):
+        for kernel in ("twide", "other"):
             buf, gs = pct.packed_grids(levels, torch.float32)
             # no slabs: the small grids' axes would go to the slab kernel
             b = pct.Batch(gs, levels, lmin, lmax, wavelet, compensated=True,
                           slabs=False)
             for forward in (True, False):
-                cls = {c: kernel for c, _, names, _ in b.tuning(forward)
+                # the other kernel: the wide kernel, or for pencils of 8
+                # and 16 chunks the tile kernel
+                cls = {c: kernel if kernel == "twide" else
+                       "wide" if "wide" in names else "tile"
+                       for c, _, names, _ in b.tuning(forward)
                        if "twide" in names}
                 assert cls, "no class of the scheme takes the TMA wide kernel"
                 b.set_tuning(cls, forward)
-                assert all(ch == kernel for c, _, _, ch in b.tuning(forward)
+                assert all(ch == cls[c] for c, _, _, ch in b.tuning(forward)
                            if c in cls)
                 if kernel == "twide":
                     seen.update(d["log2_n"] for c, d, _, _ in
@@ -533,7 +539,7 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
             s.synchronize()
             b.status()
             out.append((fwd, buf.clone()))
-            if kernel == "wide":
+            if kernel == "other":
                 c0 = b.tuning(True)[0][0]
                 with pytest.raises(ValueError):
                     b.set_tuning({c0: "twide", 1 << 20: "wide"})
@@ -542,5 +548,5 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
             b.close()
         assert torch.equal(out[0][0], out[1][0]), wavelet
         assert torch.equal(out[0][1], out[1][1]), wavelet
-    # pencils of 4 to 64 points (axes at level 1 = lmin have nothing to do)
-    assert {2, 3, 4, 5, 6} <= seen, seen
+    # pencils of 4 to 256 points (axes at level 1 = lmin have nothing to do)
+    assert {2, 3, 4, 5, 6, 7, 8} <= seen, seen

@@ -288,22 +288,22 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // Chunk size of the TMA wide launch that may take a stage (the stage's own
 // kernel otherwise): strided wide stages (chunks of 2-16 points, up to 4 per
-// pencil) and tile stages of 8 or 16 chunks of 16 points; 0 for the rest.
+// pencil) and tile stages of 8 to 32 chunks of 16 points; 0 for the rest.
 int twide_chunk(Stage const &st) {
   int const R = st.R;
   if (R == kWide + 2 || R == kWide + 4 || R == kWide + 8 || R == kWide + 16)
     return R - kWide;
   if ((R == kTile + 16 || R == kTileLong + 16) && st.job.log2_n >= 7 &&
-      st.job.log2_n <= 8)
+      st.job.log2_n <= 9)
     return 16;
   return 0;
 }
 
 // The TMA wide job and tensor map of a strided stage (FP32c, float storage)
 // with chunks of r points: the 3D view [outer][n][inner] of the stage's
-// pencils with the axis' strides, boxes {Bx, n, Sx} covering one tile of
-// Ct = 2 NT / G columns. False when the stage does not qualify
-// (alignment, inner extent under 4 columns, more than 16 chunks, 2^30 tiles
+// pencils with the axis' strides, boxes {Bx, min(n, 256), Sx} covering one
+// tile of Ct = 2 NT / G columns. False when the stage does not qualify
+// (alignment, inner extent under 4 columns, more than 32 chunks, 2^30 tiles
 // or more, or the encoder refuses the map).
 bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
                long long &tiles) {
@@ -312,7 +312,7 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
   int const log2r = 31 - __builtin_clz(static_cast<unsigned>(r));
   int const log2G = lj.log2_n - log2r;
   if (encode == nullptr || lj.periodic != 1 || lj.base % 16 != 0 ||
-      lj.log2_inner < 2 || log2G < 0 || log2G > 4 || lj.log2_n > 8 ||
+      lj.log2_inner < 2 || log2G < 0 || log2G > 5 || lj.log2_n > 9 ||
       (log2G > 2 && r != 16))
     return false;
   int const log2ct = Log2<kTWideThreads>::value + 1 - log2G;
@@ -326,6 +326,7 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
   job.log2_bx = std::min(std::min(lj.log2_inner, log2ct), 8);
   job.log2_sx = std::max(0, log2ct - lj.log2_inner);
   job.nxb = 1 << (log2ct - job.log2_bx - job.log2_sx);
+  job.log2_nbox = std::min(lj.log2_n, 8);
   tiles = (lj.columns + (1LL << (log2ct + log2u)) - 1) >> (log2ct + log2u);
   if (tiles >= (1LL << 30)) return false;
   long long const outer = lj.columns >> lj.log2_inner;
@@ -334,7 +335,7 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
                         static_cast<cuuint64_t>(outer)};
   cuuint64_t strides[2] = {static_cast<cuuint64_t>(4) << lj.log2_kstride,
                            static_cast<cuuint64_t>(4) << lj.log2_astride};
-  cuuint32_t box[3] = {1u << job.log2_bx, 1u << lj.log2_n,
+  cuuint32_t box[3] = {1u << job.log2_bx, 1u << job.log2_nbox,
                        1u << job.log2_sx};
   cuuint32_t elem[3] = {1, 1, 1};
   CUresult const res = encode(

@@ -207,13 +207,13 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
     k.mask |= 1 << kChooseTile;
   // The TMA wide kernel: FP32c strided stages, 16-byte aligned, inner
   // extents of 4 or more columns; wide stages of up to 4 chunks, and tile
-  // stages of 8 or 16 chunks of 16 points (pencils of 128 and 256 points).
+  // stages of 8 to 32 chunks of 16 points (pencils of 128 to 512 points).
   if (!last && v.wide_last && v.log2_inner >= 2 && v.base % 16 == 0 &&
       v.columns < (1LL << 30) &&
       ((k.has(kChooseWide) &&
         v.log2_n - (31 - __builtin_clz(static_cast<unsigned>(
                              wide_chunk(v.log2_n)))) <= 2) ||
-       (k.has(kChooseTile) && log2G >= 3 && log2G <= 4)))
+       (k.has(kChooseTile) && log2G >= 3 && log2G <= 5)))
     k.mask |= 1 << kChooseTmaWide;
   // Default: the wide kernel for strided pencils (and FP32c last-axis
   // pencils: measured on 2^26-point grids, 3.0-4.5 TB/s against 2.8-4.1 on
@@ -231,7 +231,7 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   // and 256 points; at 4 points the wide kernel is faster, 5.26 against
   // 4.39-4.55 TB/s.)
   if (k.has(kChooseTmaWide) &&
-      (!k.has(kChooseWide) || wide_chunk(v.log2_n) >= 8))
+      (wide_chunk(v.log2_n) >= 8 || (!k.has(kChooseWide) && log2G <= 4)))
     k.dflt = kChooseTmaWide;
   else if (k.has(kChooseWide) && (!last || v.wide_last))
     k.dflt = kChooseWide;

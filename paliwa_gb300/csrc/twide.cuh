@@ -1,17 +1,19 @@
 // TMA wide kernel: the wide kernel's register transform (rows of two
 // adjacent columns as double-float f32x2 pairs, chunks of one pencil in
 // lanes 32 / G apart, shuffles only) for strided axes with pencils of up to
-// 256 points (G <= 16 chunks), with the data moved by the tensor memory
+// 512 points (G <= 32 chunks), with the data moved by the tensor memory
 // accelerator instead of per-thread copies.
 //
 // A tile is one unit of the wide kernel: NT threads x R rows x 2 columns =
 // Ct = 2 NT / G consecutive columns (column = (outer index, inner index)) of
 // all n rows of their pencils. Each grid and axis has a 3D tensor map over
 // its [outer][n][inner] view (strides of the axis: sub-lattices included);
-// a tile is 1 or 2 boxes {Bx columns of one outer index, n rows, Sx outer
-// indices} (Bx = min(inner, Ct, 256), Sx = Ct / inner when inner < Ct),
-// loaded into shared memory as [box][outer][row][column], completion on an
-// mbarrier with a bounded wait. Every box starts on a 128-byte boundary of
+// a tile is 1 or 2 column boxes {Bx columns of one outer index, Sx outer
+// indices} (Bx = min(inner, Ct, 256), Sx = Ct / inner when inner < Ct) of
+// n rows, in boxes of at most 256 rows (the tensor memory accelerator's
+// limit per box dimension), loaded into shared memory as
+// [column box][row box][outer][row][column], completion on an mbarrier with
+// a bounded wait. Every box starts on a 128-byte boundary of
 // shared memory, as bulk tensor copies require; so the G chunks of a warp,
 // R rows apart, read the same banks (a G-way conflict on 8 or more chunks:
 // a pad after one box per chunk would remove it, but would move the boxes
@@ -57,8 +59,8 @@ struct TWideJob {
   int nlevels;
   int log2_bx;           // box: 2^log2_bx columns of one outer index
   int log2_sx;           // box: 2^log2_sx outer indices
-  int nxb;               // boxes per tile
-  int pad_;
+  int nxb;               // column boxes per tile
+  int log2_nbox;         // rows per box: min(n, 256)
 };
 
 struct TWideParams {
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       z += xb << job.log2_sx;
   };
   auto box_bytes = [](TWideJob const &job) {
-    return 4 << (job.log2_bx + job.log2_n + job.log2_sx);
+    return 4 << (job.log2_bx + job.log2_nbox + job.log2_sx);
   };
 
   // The producer lane issues every copy; it keeps the last map it fenced.
@@ -205,7 +207,8 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       fenced = job.map;
     }
     int const bb = box_bytes(job);
-    mbar_expect_tx(&full[b], static_cast<unsigned>(U * bb * job.nxb));
+    int const nc = 1 << (job.log2_n - job.log2_nbox);  // row boxes
+    mbar_expect_tx(&full[b], static_cast<unsigned>(U * bb * job.nxb * nc));
     for (int u = 0; u < U; ++u) {
       int x0, z0;
       origin(job, tile, u, x0, z0);
@@ -213,7 +216,9 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       for (int xb = 0; xb < job.nxb; ++xb) {
         int x, z;
         box_at(job, xb, x0, z0, x, z);
-        tma_load_3d(dst + xb * bb, map, x, 0, z, &full[b]);
+        for (int cb = 0; cb < nc; ++cb)
+          tma_load_3d(dst + (xb * nc + cb) * bb, map, x, cb << job.log2_nbox,
+                      z, &full[b]);
       }
     }
   };
@@ -223,6 +228,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     TWideJob const &job = sjob[b];
     void const *const map = p.maps + job.map;
     int const bb = box_bytes(job);
+    int const nc = 1 << (job.log2_n - job.log2_nbox);
     for (int u = 0; u < U; ++u) {
       int x0, z0;
       origin(job, tile, u, x0, z0);
@@ -230,7 +236,9 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       for (int xb = 0; xb < job.nxb; ++xb) {
         int x, z;
         box_at(job, xb, x0, z0, x, z);
-        tma_store_3d(map, x, 0, z, src + xb * bb);
+        for (int cb = 0; cb < nc; ++cb)
+          tma_store_3d(map, x, cb << job.log2_nbox, z,
+                       src + (xb * nc + cb) * bb);
       }
     }
     bulk_commit();
@@ -286,9 +294,8 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     // Thread = (chunk c, column pair g): the chunks of a column pair are
     // lanes W = 32 / G apart, the W column pairs of one chunk consecutive.
     int const log2G = job.log2_n - LOG2R;
-    // The planner gives at most 16 chunks per pencil; more than 32 would
-    // take the exchange paths that need a CTA barrier, which this kernel
-    // has not.
+    // The planner gives at most 32 chunks per pencil; more would take the
+    // exchange paths that need a CTA barrier, which this kernel has not.
     if (static_cast<unsigned>(log2G) <= 5u) {
       int const log2W = 5 - log2G;
       int const c = lane >> log2W;
@@ -299,10 +306,15 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       int const rem = col & ((1 << log2bs) - 1);
       int const s = rem >> job.log2_bx;
       int const bcol = rem & ((1 << job.log2_bx) - 1);
+      // The box holding row c R of the thread's columns (its R rows lie in
+      // one box: 256 is a multiple of R), and that row in the box
+      int const r0 = c << LOG2R;
+      int const box = (xb << (job.log2_n - job.log2_nbox)) +
+                      (r0 >> job.log2_nbox);
+      int const jr = r0 & ((1 << job.log2_nbox) - 1);
       // float index of row c R of the thread's columns; rows are Bx apart
-      int const idx0 = (xb << (log2bs + job.log2_n)) +
-                       ((((s << job.log2_n) + (c << LOG2R)) << job.log2_bx) +
-                        bcol);
+      int const idx0 = (box << (log2bs + job.log2_nbox)) +
+                       ((((s << job.log2_nbox) + jr) << job.log2_bx) + bcol);
       for (int u = 0; u < U; ++u) {
         float *const tf =
             reinterpret_cast<float *>(tiles + b * TILE + u * UNIT);

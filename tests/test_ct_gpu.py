@@ -489,17 +489,17 @@ def test_tma_wide_kernel_gives_the_wide_kernels_bits():
 
 
 def test_every_tma_wide_class_gives_the_wide_kernels_bits():
-    """Chunks of 2, 4, 8 and 16 points, up to 16 chunks per pencil: every
+    """Chunks of 2, 4, 8 and 16 points, up to 32 chunks per pencil: every
     class of stages that the TMA wide kernel applies to, set to it through
     set_tuning, gives the bits of the same classes set to the per-thread-copy
-    wide kernel (or, for pencils of 128 and 256 points, the tile kernel),
+    wide kernel (or, for pencils of 128 to 512 points, the tile kernel),
     forward and inverse, for every wavelet. A kernel that does not apply, or
     a class the plan lacks, is refused with nothing changed."""
     import torch
     levels = [(6, 1, 3), (5, 2, 2), (4, 6, 1), (3, 3, 5), (6, 6, 2), (2, 5, 7),
               (1, 4, 9), (6, 2, 1), (2, 2, 2), (5, 5, 5), (4, 1, 10),
               (3, 2, 8), (2, 3, 6), (7, 4, 3), (8, 5, 1), (2, 8, 4),
-              (7, 2, 2), (13, 2, 1)]
+              (7, 2, 2), (13, 2, 1), (9, 3, 2), (2, 9, 4)]
     lmin, lmax = (1, 1, 1), (14, 14, 14)
     rng = np.random.default_rng(78)
     host = [rng.uniform(-1, 1, 1 << sum(l)).astype(np.float32)
@@ -548,5 +548,5 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
             b.close()
         assert torch.equal(out[0][0], out[1][0]), wavelet
         assert torch.equal(out[0][1], out[1][1]), wavelet
-    # pencils of 4 to 256 points (axes at level 1 = lmin have nothing to do)
-    assert {2, 3, 4, 5, 6, 7, 8} <= seen, seen
+    # pencils of 4 to 512 points (axes at level 1 = lmin have nothing to do)
+    assert {2, 3, 4, 5, 6, 7, 8, 9} <= seen, seen

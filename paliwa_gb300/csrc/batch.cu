@@ -288,23 +288,27 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // Chunk size of the TMA wide launch that may take a stage (the stage's own
 // kernel otherwise): strided wide stages (chunks of 2-16 points, up to 4 per
-// pencil) and tile stages of 8 to 32 chunks of 16 points; 0 for the rest.
+// pencil), and tile or staged stages of pencils of 128 to 2048 points (8 to
+// 128 chunks of 16 points); 0 for the rest.
 int twide_chunk(Stage const &st) {
   int const R = st.R;
   if (R == kWide + 2 || R == kWide + 4 || R == kWide + 8 || R == kWide + 16)
     return R - kWide;
-  if ((R == kTile + 16 || R == kTileLong + 16) && st.job.log2_n >= 7 &&
-      st.job.log2_n <= 9)
+  if ((R == kTile + 16 || R == kTileLong + 16 || R == 16 || R == 32) &&
+      st.job.log2_n >= 7 && st.job.log2_n <= 11)
     return 16;
   return 0;
 }
 
 // The TMA wide job and tensor map of a strided stage (FP32c, float storage)
-// with chunks of r points: the 3D view [outer][n][inner] of the stage's
-// pencils with the axis' strides, boxes {Bx, min(n, 256), Sx} covering one
-// tile of Ct = 2 NT / G columns. False when the stage does not qualify
-// (alignment, inner extent under 4 columns, more than 32 chunks, 2^30 tiles
-// or more, or the encoder refuses the map).
+// with chunks of r points, covering tiles of Ct = 2 NT / G columns. Up to 4
+// chunks per pencil: the 3D view [outer][n][inner] of the stage's pencils
+// with the axis' strides and boxes {Bx, n, Sx}. 8 to 128 chunks of 16
+// points (the chunked layout): the 5D view [outer][inner / 4][row of
+// chunk][chunk][4 columns] and one box per tile, so that shared memory holds
+// the tile as [column quad][row of chunk][chunk][4 columns]. False when the
+// stage does not qualify (alignment, inner extent under 4 columns, more than
+// 128 chunks, 2^30 tiles or more, or the encoder refuses the map).
 bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
                long long &tiles) {
   auto encode = tensor_map_encoder();
@@ -312,7 +316,7 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
   int const log2r = 31 - __builtin_clz(static_cast<unsigned>(r));
   int const log2G = lj.log2_n - log2r;
   if (encode == nullptr || lj.periodic != 1 || lj.base % 16 != 0 ||
-      lj.log2_inner < 2 || log2G < 0 || log2G > 5 || lj.log2_n > 9 ||
+      lj.log2_inner < 2 || log2G < 0 || log2G > 7 || lj.log2_n > 11 ||
       (log2G > 2 && r != 16))
     return false;
   int const log2ct = Log2<kTWideThreads>::value + 1 - log2G;
@@ -330,6 +334,30 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
   tiles = (lj.columns + (1LL << (log2ct + log2u)) - 1) >> (log2ct + log2u);
   if (tiles >= (1LL << 30)) return false;
   long long const outer = lj.columns >> lj.log2_inner;
+  if (log2G >= 3) {
+    job.chunked = 1;
+    job.nxb = 1;
+    job.log2_nbox = lj.log2_n;
+    job.log2_bx = std::min(lj.log2_inner, log2ct);  // Bx >= 4: log2ct <= 6
+    job.log2_sx = log2ct - job.log2_bx;
+    cuuint64_t dims[5] = {4, static_cast<cuuint64_t>(1) << log2G,
+                          static_cast<cuuint64_t>(r),
+                          static_cast<cuuint64_t>(1) << (lj.log2_inner - 2),
+                          static_cast<cuuint64_t>(outer)};
+    cuuint64_t strides[4] = {
+        static_cast<cuuint64_t>(4 * r) << lj.log2_kstride,
+        static_cast<cuuint64_t>(4) << lj.log2_kstride, 16,
+        static_cast<cuuint64_t>(4) << lj.log2_astride};
+    cuuint32_t box[5] = {4, 1u << log2G, static_cast<cuuint32_t>(r),
+                         1u << (job.log2_bx - 2), 1u << job.log2_sx};
+    cuuint32_t elem[5] = {1, 1, 1, 1, 1};
+    CUresult const res = encode(
+        &map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5,
+        reinterpret_cast<void *>(lj.base), dims, strides, box, elem,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return res == CUDA_SUCCESS;
+  }
   cuuint64_t dims[3] = {static_cast<cuuint64_t>(1) << lj.log2_inner,
                         static_cast<cuuint64_t>(1) << lj.log2_n,
                         static_cast<cuuint64_t>(outer)};
@@ -436,7 +464,9 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
             int const r = twide_chunk(st);
             if (tma && st.tma && r > 0 &&
                 canonical_shifts(st.job, (ws & 1) != 0))
-              code = kTWide + r;
+              code = kTWide + r +
+                     (st.job.log2_n - (31 - __builtin_clz(r)) > 5 ? kTWideLong
+                                                                  : 0);
             by_r[code].push_back(&st);
           }
         for (auto const &[R, list] : by_r) {
@@ -453,7 +483,8 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
               TWideJob job;
               CUtensorMap map;
               long long tiles = 0;
-              if (!twide_job(*st, R - kTWide, job, map, tiles)) {
+              if (!twide_job(*st, (R - kTWide) % kTWideLong, job, map,
+                             tiles)) {
                 rest[st->R].push_back(st);
                 continue;
               }

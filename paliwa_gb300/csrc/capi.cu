@@ -206,14 +206,14 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
           tile_piece_log2(log2G, v.log2_row + v.log2_es))
     k.mask |= 1 << kChooseTile;
   // The TMA wide kernel: FP32c strided stages, 16-byte aligned, inner
-  // extents of 4 or more columns; wide stages of up to 4 chunks, and tile
-  // stages of 8 to 32 chunks of 16 points (pencils of 128 to 512 points).
+  // extents of 4 or more columns; wide stages of up to 4 chunks, and
+  // pencils of 8 to 128 chunks of 16 points (128 to 2048 points).
   if (!last && v.wide_last && v.log2_inner >= 2 && v.base % 16 == 0 &&
       v.columns < (1LL << 30) &&
       ((k.has(kChooseWide) &&
         v.log2_n - (31 - __builtin_clz(static_cast<unsigned>(
                              wide_chunk(v.log2_n)))) <= 2) ||
-       (k.has(kChooseTile) && log2G >= 3 && log2G <= 5)))
+       (R == 16 && log2G >= 3 && log2G <= 7)))
     k.mask |= 1 << kChooseTmaWide;
   // Default: the wide kernel for strided pencils (and FP32c last-axis
   // pencils: measured on 2^26-point grids, 3.0-4.5 TB/s against 2.8-4.1 on
@@ -225,15 +225,14 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   // the staged kernel); then the direct kernel, then the staged one.
   int const tile_log2G_max = v.wide_last ? 4 : v.log2_es == 3 ? 5 : 8;
   // (The TMA wide kernel is the default for wide chunks of 8 and 16 points
-  // and for pencils of 8 or 16 chunks, where it measured faster per launch
+  // and for pencils of 8 to 32 chunks, where it measured faster per launch
   // on the 4D CT batch: 4.73 against 4.01 TB/s at 8 points, 4.73 against
   // 3.16 at 16, about 3.7 against 2.29 on the tile kernel's pencils of 128
-  // and 256 points; at 4 points the wide kernel is faster, 5.26 against
-  // 4.39-4.55 TB/s.)
-  if (k.has(kChooseTmaWide) &&
-      (wide_chunk(v.log2_n) >= 8 || (!k.has(kChooseWide) && log2G <= 4)))
-    k.dflt = kChooseTmaWide;
-  else if (k.has(kChooseWide) && (!last || v.wide_last))
+  // and 256 points, 0.46 against 0.71 ms on the staged kernel's pencils of
+  // 512; at 4 points the wide kernel is faster, 5.26 against 4.39-4.55
+  // TB/s, and on pencils of 1024 and 2048 points, whose chunks exchange
+  // through shared memory, the staged kernel: 2.2 against 2.6 TB/s.)
+  if (k.has(kChooseWide) && (!last || v.wide_last))
     k.dflt = kChooseWide;
   else if (k.has(kChooseTile) && log2G <= tile_log2G_max)
     k.dflt = kChooseTile;
@@ -241,6 +240,10 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
     k.dflt = kChooseDirect;
   else
     k.dflt = staged_chunk(v) == 32 ? kChooseStaged32 : kChooseStaged;
+  k.fallback = k.dflt;
+  if (k.has(kChooseTmaWide) &&
+      (wide_chunk(v.log2_n) >= 8 || (!k.has(kChooseWide) && log2G <= 5)))
+    k.dflt = kChooseTmaWide;
   return k;
 }
 
@@ -289,16 +292,13 @@ void plan_periodic(AxisView const &v, std::vector<int> const &shifts, int ws,
       st.job.col_tiles =
           ceil_div(v.columns >> v.log2_row, kThreads >> log2G);
     };
-    switch (choice) {
-    case kChooseTmaWide:
+    if (choice == kChooseTmaWide) {
       // Marked for the TMA wide kernel (batches); elsewhere, and for the
-      // grids that do not qualify, the kernel it stands in for.
+      // grids that do not qualify, planned for the kernel it stands in for.
       st.tma = true;
-      if (!ks.has(kChooseWide)) {
-        tile_stage();
-        break;
-      }
-      [[fallthrough]];
+      choice = ks.fallback;
+    }
+    switch (choice) {
     case kChooseWide:
       if (last) {
         st.R = kWideContig + R;

@@ -213,9 +213,15 @@ __device__ __forceinline__ int tile_pitch(int G, int log2_inner,
 // 2^log2ls apart (the wide kernel, whose neighbouring lanes hold
 // neighbouring columns). Longer columns exchange through shared memory with
 // one barrier per step (the same for every thread of the CTA: G is uniform
-// per tile).
-template <class A, int NT> struct RoundCtx {
+// per tile). BAR = 0: the barrier is the CTA's; BAR > 0: named barrier BAR
+// among the NT threads that transform (a CTA whose other warps copy).
+// SHFL: the caller guarantees G <= 32 (the shared-memory paths compile out).
+__device__ __forceinline__ void named_barrier(int id, int count) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
+}
+template <class A, int NT, int BAR = 0, bool SHFL = false> struct RoundCtx {
   using V = typename A::V;
+  static constexpr bool kShflOnly = SHFL;
   // Chunk heads of one column are consecutive threads (coarse_heads may
   // run a column's coarse levels as a pencil of heads in one warp).
   static constexpr bool kHeadPencil = true;
@@ -234,15 +240,21 @@ template <class A, int NT> struct RoundCtx {
   __device__ __forceinline__ int chunk_lane(int cc) const {
     return gbase_lane | ((cc & (G - 1)) << log2ls);
   }
+  __device__ __forceinline__ void sync() const {
+    if constexpr (BAR == 0)
+      __syncthreads();
+    else
+      named_barrier(BAR, NT);
+  }
 
   // The neighbour of a fine step: slot 0 of the next chunk (o = 1) or slot
   // R - s of the previous chunk (o = 0); `pub` is this chunk's value of it.
   __device__ __forceinline__ V fine_neighbor(int o, V pub) {
     if (G == 1) return pub;
     int nc = (o == 1) ? c + 1 : c - 1;
-    if (G <= 32) return shfl(pub, chunk_lane(nc));
+    if (SHFL || G <= 32) return shfl(pub, chunk_lane(nc));
     xch[buf * NT + t] = pub;
-    __syncthreads();
+    sync();
     if (periodic)
       nc &= G - 1;
     else
@@ -259,7 +271,7 @@ template <class A, int NT> struct RoundCtx {
   template <class Upd>
   __device__ __forceinline__ void coarse(V &v0, int o, int d, Upd upd) {
     bool const mine = (c & (2 * d - 1)) == o * d;
-    if (G <= 32) {
+    if (SHFL || G <= 32) {
       V const lo = shfl(v0, chunk_lane(c - d));
       V const up = shfl(v0, chunk_lane(c + d));
       if (mine) v0 = upd(lo, v0, up);
@@ -267,7 +279,7 @@ template <class A, int NT> struct RoundCtx {
     }
     if (!heads_valid) {
       heads[t] = v0;
-      __syncthreads();
+      sync();
       heads_valid = true;
     }
     if (mine) {
@@ -283,7 +295,7 @@ template <class A, int NT> struct RoundCtx {
       v0 = upd(heads[colbase + cl], v0, heads[colbase + cu]);
       heads[t] = v0;
     }
-    __syncthreads();
+    sync();
   }
 };
 
@@ -554,13 +566,13 @@ template <int W, bool FWD> struct WaveletSched {
   static __device__ __forceinline__ bool coarse_heads(typename A::V &head,
                                                       Ctx &ctx,
                                                       int Lc) {
-    if constexpr (R < 16 || !Ctx::kHeadPencil) {
+    if constexpr (R < 16 || !Ctx::kHeadPencil || Ctx::kShflOnly) {
       return false;
     } else {
       if (ctx.G <= 32 || ctx.G > 256) return false;
       using V = typename A::V;
       ctx.heads[ctx.t] = head;
-      __syncthreads();
+      ctx.sync();
       int const w = ctx.t >> 5;
       int const lane = ctx.t & 31;
       if (w < (NT >> ctx.log2G)) {  // one warp per column of the round
@@ -571,7 +583,7 @@ template <int W, bool FWD> struct WaveletSched {
         case 256: head_pencil<8, A, NT>(col, lane, ctx.periodic, Lc); break;
         }
       }
-      __syncthreads();
+      ctx.sync();
       head = ctx.heads[ctx.t];
       ctx.heads_valid = false;
       return true;

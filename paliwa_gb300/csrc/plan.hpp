@@ -111,6 +111,10 @@ enum KernelChoice {
 struct KernelSet {
   unsigned mask = 0;  // a bit per applicable KernelChoice
   int dflt = kChooseStaged;
+  // The kernel that a stage choosing kChooseTmaWide is planned for (the
+  // wide kernel, else the default without the TMA wide kernel): it runs the
+  // stage outside batches and where the tensor map cannot be made.
+  int fallback = kChooseStaged;
   bool has(int c) const { return (mask >> c) & 1u; }
 };
 struct Tuning {

@@ -148,6 +148,8 @@ __device__ __forceinline__ int swz128(int b) {
 template <class A, int NT> struct SlabCtx {
   using V = typename A::V;
   static constexpr bool kHeadPencil = false;
+  static constexpr bool kShflOnly = false;
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
   int t, c, G, log2G, log2ls, gbase_lane, cbase;
   bool in_warp;
   int periodic = 1;

@@ -50,6 +50,9 @@ namespace pgb {
 
 constexpr int kTWideThreads = 256;               // transform threads
 constexpr int kTWideBlock = kTWideThreads + 32;  // + the producer warp
+// Added to the chunk size of a launch whose pencils have more than 32
+// chunks (the LONG kernel).
+constexpr int kTWideLong = 64;
 
 struct TWideJob {
   long long tile_begin;  // first tile of this job in the launch
@@ -61,6 +64,7 @@ struct TWideJob {
   int log2_sx;           // box: 2^log2_sx outer indices
   int nxb;               // column boxes per tile
   int log2_nbox;         // rows per box: min(n, 256)
+  int chunked;           // 1: the chunk-interleaved layout (G >= 8)
 };
 
 struct TWideParams {
@@ -109,8 +113,45 @@ template <int R> struct TWideShape {
       size_t(kStages) * kTileBytes + 128;  // + 128-byte alignment slack
 };
 
-template <int R> constexpr size_t twide_smem_bytes() {
-  return TWideShape<R>::kSmemBytes;
+// Launches with pencils of more than 32 chunks also hold the exchange
+// buffers of their chunk heads (NT rows) and fine steps (2 NT rows).
+template <int R, bool LONG> constexpr size_t twide_smem_bytes() {
+  return TWideShape<R>::kSmemBytes + (LONG ? 3 * kTWideThreads * 16 : 0);
+}
+
+__device__ __forceinline__ void tma_load_5d(void *dst, void const *map,
+                                            int q, int z, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx"
+      "::bytes [%0], [%1, {%2, %2, %2, %3, %4}], [%5];\n" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(0), "r"(q), "r"(z),
+      "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_5d(void const *map, int q, int z,
+                                             void const *src) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.global.shared::cta.bulk_group [%0, {%1, %1, "
+      "%1, %2, %3}], [%4];\n" ::"l"(reinterpret_cast<unsigned long long>(map)),
+      "r"(0), "r"(q), "r"(z), "r"(smem_u32(src))
+      : "memory");
+}
+
+// True on every participating thread when `v` is true on all NT of them
+// (named barrier `id`).
+__device__ __forceinline__ bool named_barrier_and(int id, int count, bool v) {
+  unsigned r;
+  asm volatile(
+      "{\n"
+      ".reg .pred p, q;\n"
+      "setp.ne.u32 p, %1, 0;\n"
+      "bar.red.and.pred q, %2, %3, p;\n"
+      "selp.u32 %0, 1, 0, q;\n"
+      "}\n"
+      : "=r"(r)
+      : "r"(static_cast<unsigned>(v)), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -131,7 +172,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
   return true;
 }
 
-template <class A, int R, class Sched>
+// LONG: every job of the launch has pencils of 64 or 128 chunks (1024 and
+// 2048 points), held by consecutive threads, whose exchanges go through
+// shared memory under named barrier 1 among the NT transform threads (the
+// producer warp never takes part); otherwise pencils of at most 32 chunks,
+// exchanging by shuffles, and no barrier after the start.
+template <class A, int R, class Sched, bool LONG>
 __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     twide_kernel(__grid_constant__ const TWideParams p) {
   using V = typename A::V;
@@ -148,6 +194,8 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
   unsigned const base_addr = smem_u32(smem_raw);
   unsigned char *const tiles =
       smem_raw + ((128 - (base_addr & 127)) & 127);  // 128-byte aligned
+  V *const heads = reinterpret_cast<V *>(tiles + S * TILE);  // LONG only
+  V *const xch = heads + NT;
   __shared__ uint64_t full[S], empty[S];
   __shared__ TWideJob sjob[S];
   __shared__ int abort_flag;  // set when a bounded wait gave up
@@ -213,6 +261,10 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       int x0, z0;
       origin(job, tile, u, x0, z0);
       unsigned char *const dst = tiles + b * TILE + u * UNIT;
+      if (job.chunked) {  // one box: the unit (nxb = nc = 1)
+        tma_load_5d(dst, map, x0 >> 2, z0, &full[b]);
+        continue;
+      }
       for (int xb = 0; xb < job.nxb; ++xb) {
         int x, z;
         box_at(job, xb, x0, z0, x, z);
@@ -233,6 +285,10 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       int x0, z0;
       origin(job, tile, u, x0, z0);
       unsigned char const *const src = tiles + b * TILE + u * UNIT;
+      if (job.chunked) {
+        tma_store_5d(map, x0 >> 2, z0, src);
+        continue;
+      }
       for (int xb = 0; xb < job.nxb; ++xb) {
         int x, z;
         box_at(job, xb, x0, z0, x, z);
@@ -282,8 +338,14 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     int const b = static_cast<int>(k % S);
     bool const ok = mbar_wait_bounded(
         &full[b], static_cast<unsigned>((k / S) & 1), abort);
-    // A warp leaves as a whole (its lanes exchange by shuffles).
-    if (!__all_sync(0xffffffffu, ok)) {
+    // Threads that exchange leave together: a warp (shuffles), or with
+    // LONG all transform threads (named barriers).
+    bool all_ok;
+    if constexpr (LONG)
+      all_ok = named_barrier_and(1, NT, ok);
+    else
+      all_ok = __all_sync(0xffffffffu, ok);
+    if (!all_ok) {
       if (lane == 0) {
         atomicExch(p.error, 1u);
         *abort = 1;
@@ -291,30 +353,54 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       break;
     }
     TWideJob const &job = sjob[b];
-    // Thread = (chunk c, column pair g): the chunks of a column pair are
-    // lanes W = 32 / G apart, the W column pairs of one chunk consecutive.
     int const log2G = job.log2_n - LOG2R;
-    // The planner gives at most 32 chunks per pencil; more would take the
-    // exchange paths that need a CTA barrier, which this kernel has not.
-    if (static_cast<unsigned>(log2G) <= 5u) {
-      int const log2W = 5 - log2G;
-      int const c = lane >> log2W;
-      int const g = ((t >> 5) << log2W) | (lane & ((1 << log2W) - 1));
-      int const col = 2 * g;
-      int const log2bs = job.log2_bx + job.log2_sx;
-      int const xb = col >> log2bs;
-      int const rem = col & ((1 << log2bs) - 1);
-      int const s = rem >> job.log2_bx;
-      int const bcol = rem & ((1 << job.log2_bx) - 1);
-      // The box holding row c R of the thread's columns (its R rows lie in
-      // one box: 256 is a multiple of R), and that row in the box
-      int const r0 = c << LOG2R;
-      int const box = (xb << (job.log2_n - job.log2_nbox)) +
-                      (r0 >> job.log2_nbox);
-      int const jr = r0 & ((1 << job.log2_nbox) - 1);
-      // float index of row c R of the thread's columns; rows are Bx apart
-      int const idx0 = (box << (log2bs + job.log2_nbox)) +
-                       ((((s << job.log2_nbox) + jr) << job.log2_bx) + bcol);
+    // Jobs as the planner makes them: LONG launches 64 or 128 chunks of 16
+    // points in the chunked layout, the others at most 32 chunks (the
+    // exchange paths of longer pencils need the named barriers). The test
+    // is uniform over the tile, so every thread takes the same barriers.
+    bool const valid =
+        LONG ? (R == 16 && job.chunked && log2G >= 6 && log2G <= 7)
+             : (static_cast<unsigned>(log2G) <= 5u &&
+                (!job.chunked || (R == 16 && log2G >= 3)));
+    if (valid) {
+      int const G = 1 << log2G;
+      // Thread = (chunk c, column pair g). Up to 32 chunks: the chunks of a
+      // column pair are lanes W = 32 / G apart, the W column pairs of one
+      // chunk consecutive; more: chunks in consecutive threads.
+      int c, g, log2ls;
+      if (!LONG) {
+        log2ls = 5 - log2G;
+        c = lane >> log2ls;
+        g = ((t >> 5) << log2ls) | (lane & ((1 << log2ls) - 1));
+      } else {
+        log2ls = 0;
+        c = t & (G - 1);
+        g = t >> log2G;
+      }
+      // Float index of the thread's row j: idx0 + j * rstride.
+      int idx0, log2rs;
+      if (LONG || job.chunked) {
+        // [column quad][row of chunk][chunk][4 columns]
+        idx0 = (((((g >> 1) << LOG2R) << log2G) + c) << 2) + 2 * (g & 1);
+        log2rs = log2G + 2;
+      } else {
+        int const col = 2 * g;
+        int const log2bs = job.log2_bx + job.log2_sx;
+        int const xb = col >> log2bs;
+        int const rem = col & ((1 << log2bs) - 1);
+        int const s = rem >> job.log2_bx;
+        int const bcol = rem & ((1 << job.log2_bx) - 1);
+        // The box holding row c R of the thread's columns (its R rows lie
+        // in one box: 256 is a multiple of R), and that row in the box
+        int const r0 = c << LOG2R;
+        int const box = (xb << (job.log2_n - job.log2_nbox)) +
+                        (r0 >> job.log2_nbox);
+        int const jr = r0 & ((1 << job.log2_nbox) - 1);
+        // [box][outer][row][column]: rows are Bx apart
+        idx0 = (box << (log2bs + job.log2_nbox)) +
+               ((((s << job.log2_nbox) + jr) << job.log2_bx) + bcol);
+        log2rs = job.log2_bx;
+      }
       for (int u = 0; u < U; ++u) {
         float *const tf =
             reinterpret_cast<float *>(tiles + b * TILE + u * UNIT);
@@ -322,14 +408,14 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
 #pragma unroll
         for (int j = 0; j < R; ++j)
           v[j] = A::load(
-              *reinterpret_cast<W const *>(tf + idx0 + (j << job.log2_bx)));
-        RoundCtx<A, NT> ctx(t, c, 1 << log2G, log2G, lane, 1, nullptr,
-                            nullptr, log2W);
+              *reinterpret_cast<W const *>(tf + idx0 + (j << log2rs)));
+        RoundCtx<A, NT, 1, !LONG> ctx(t, c, G, log2G, lane, 1,
+                                      LONG ? heads : nullptr,
+                                      LONG ? xch : nullptr, log2ls);
         Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
 #pragma unroll
         for (int j = 0; j < R; ++j)
-          *reinterpret_cast<W *>(tf + idx0 + (j << job.log2_bx)) =
-              A::store(v[j]);
+          *reinterpret_cast<W *>(tf + idx0 + (j << log2rs)) = A::store(v[j]);
       }
     } else if (lane == 0) {
       atomicExch(p.error, 1u);

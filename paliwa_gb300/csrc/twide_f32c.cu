@@ -7,11 +7,11 @@ namespace pgb {
 
 namespace {
 
-template <int R, class Sched>
+template <int R, class Sched, bool LONG>
 void launch_twide_r(TWideParams const &p, cudaStream_t s) {
   static thread_local Occupancy occ;
-  auto kernel = twide_kernel<RowF32C, R, Sched>;
-  size_t const smem = twide_smem_bytes<R>();
+  auto kernel = twide_kernel<RowF32C, R, Sched, LONG>;
+  size_t const smem = twide_smem_bytes<R, LONG>();
   int const dev = current_device();
   if (dev < 0 || dev >= Occupancy::kMaxDevices)
     throw StatusError(2, "device ordinal beyond the launch cache");
@@ -39,17 +39,19 @@ void launch_twide_r(TWideParams const &p, cudaStream_t s) {
 template <class Sched>
 void by_r(int R, TWideParams const &p, cudaStream_t s) {
   switch (R) {
-  case 2: return launch_twide_r<2, Sched>(p, s);
-  case 4: return launch_twide_r<4, Sched>(p, s);
-  case 8: return launch_twide_r<8, Sched>(p, s);
-  case 16: return launch_twide_r<16, Sched>(p, s);
+  case 2: return launch_twide_r<2, Sched, false>(p, s);
+  case 4: return launch_twide_r<4, Sched, false>(p, s);
+  case 8: return launch_twide_r<8, Sched, false>(p, s);
+  case 16: return launch_twide_r<16, Sched, false>(p, s);
+  case kTWideLong + 16: return launch_twide_r<16, Sched, true>(p, s);
   }
   throw StatusError(2, "twide launch with an unsupported chunk size");
 }
 
 } // namespace
 
-// sched = 2 * wavelet + (forward ? 1 : 0); R = rows per chunk.
+// sched = 2 * wavelet + (forward ? 1 : 0); R = rows per chunk, plus
+// kTWideLong for pencils of more than 32 chunks.
 void launch_twide_f32c(int sched, int R, TWideParams const &p,
                        cudaStream_t s) {
   switch (sched) {

@@ -489,17 +489,18 @@ def test_tma_wide_kernel_gives_the_wide_kernels_bits():
 
 
 def test_every_tma_wide_class_gives_the_wide_kernels_bits():
-    """Chunks of 2, 4, 8 and 16 points, up to 32 chunks per pencil: every
+    """Chunks of 2, 4, 8 and 16 points, up to 128 chunks per pencil: every
     class of stages that the TMA wide kernel applies to, set to it through
     set_tuning, gives the bits of the same classes set to the per-thread-copy
-    wide kernel (or, for pencils of 128 to 512 points, the tile kernel),
-    forward and inverse, for every wavelet. A kernel that does not apply, or
-    a class the plan lacks, is refused with nothing changed."""
+    wide kernel (or, for pencils of 128 to 2048 points, the tile or staged
+    kernel), forward and inverse, for every wavelet. A kernel that does not
+    apply, or a class the plan lacks, is refused with nothing changed."""
     import torch
     levels = [(6, 1, 3), (5, 2, 2), (4, 6, 1), (3, 3, 5), (6, 6, 2), (2, 5, 7),
               (1, 4, 9), (6, 2, 1), (2, 2, 2), (5, 5, 5), (4, 1, 10),
               (3, 2, 8), (2, 3, 6), (7, 4, 3), (8, 5, 1), (2, 8, 4),
-              (7, 2, 2), (13, 2, 1), (9, 3, 2), (2, 9, 4)]
+              (7, 2, 2), (13, 2, 1), (9, 3, 2), (2, 9, 4), (10, 2, 3),
+              (3, 11, 2), (11, 1, 4)]
     lmin, lmax = (1, 1, 1), (14, 14, 14)
     rng = np.random.default_rng(78)
     host = [rng.uniform(-1, 1, 1 << sum(l)).astype(np.float32)
@@ -513,10 +514,11 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
             b = pct.Batch(gs, levels, lmin, lmax, wavelet, compensated=True,
                           slabs=False)
             for forward in (True, False):
-                # the other kernel: the wide kernel, or for pencils of 8
-                # and 16 chunks the tile kernel
+                # the other kernel: the wide kernel, else the tile or the
+                # staged kernel
                 cls = {c: kernel if kernel == "twide" else
-                       "wide" if "wide" in names else "tile"
+                       next(k for k in ("wide", "tile", "staged32", "staged")
+                            if k in names)
                        for c, _, names, _ in b.tuning(forward)
                        if "twide" in names}
                 assert cls, "no class of the scheme takes the TMA wide kernel"
@@ -530,6 +532,9 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
             kernels = b.profile(True, stream=s)[2]
             assert any(k > pct.TWIDE_KERNEL for k in kernels) == \
                 (kernel == "twide")
+            if kernel == "twide":  # pencils of 64 and 128 chunks
+                assert any(k > pct.TWIDE_KERNEL + pct.TWIDE_LONG
+                           for k in kernels)
             for g, h in zip(gs, host):
                 g.copy_(torch.from_numpy(h))
             b.hierarchize(s)
@@ -548,5 +553,5 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
             b.close()
         assert torch.equal(out[0][0], out[1][0]), wavelet
         assert torch.equal(out[0][1], out[1][1]), wavelet
-    # pencils of 4 to 512 points (axes at level 1 = lmin have nothing to do)
-    assert {2, 3, 4, 5, 6, 7, 8, 9} <= seen, seen
+    # pencils of 4 to 2048 points (axes at level 1 = lmin have nothing to do)
+    assert {2, 3, 4, 5, 6, 7, 8, 9, 10, 11} <= seen, seen

@@ -793,11 +793,12 @@ def run_axis_probe(spec):
 
 def run_batch_probe(spec):
     """One direction of a smaller 4D combination batch, for kernel captures
-    of a few GB: ``LEVEL_SUM:MODE[:noslabs]`` (MODE f64, f32 or f32c; e.g.
-    ``19:f32c``, 709 M points, 2.8 GB) builds the 4D scheme at |l|_1 =
+    of a few GB: ``LEVEL_SUM:MODE[:noslabs][:tma]`` (MODE f64, f32 or f32c;
+    e.g. ``19:f32c``, 709 M points, 2.8 GB) builds the 4D scheme at |l|_1 =
     LEVEL_SUM - q (q <= 3, lmin 1, CDF biorthogonal) on random values with
-    the planner's default kernels, runs the forward direction launch by
-    launch (no graph, plan order, one stream) and prints one JSON line per
+    the planner's default kernels (``tma``: every class of stages that the
+    TMA wide kernel applies to set to it), runs the forward direction launch
+    by launch (no graph, plan order, one stream) and prints one JSON line per
     launch: index, kernel, algorithmic bytes and event-timed milliseconds.
     The k-th launch of a kernel in that list is the k-th one a profiler
     filtered on the kernel's name sees."""
@@ -806,7 +807,8 @@ def run_batch_probe(spec):
     from paliwa_gb300 import ct as pct
     parts = spec.split(":")
     level_sum, mode = int(parts[0]), parts[1]
-    slabs = not (len(parts) > 2 and parts[2] == "noslabs")
+    slabs = "noslabs" not in parts[2:]
+    tma_all = "tma" in parts[2:]
     levels, _ = pct.combination_scheme(4, level_sum, 3, 1)
     dt = torch.float64 if mode == "f64" else torch.float32
     buf, views = pct.packed_grids(levels, dt)
@@ -814,6 +816,9 @@ def run_batch_probe(spec):
     top = level_sum - 3
     bt = pct.Batch(views, levels, (1,) * 4, (top,) * 4, "biorthogonal",
                    compensated=(mode == "f32c"), slabs=slabs)
+    if tma_all:
+        bt.set_tuning({c: "twide" for c, _, names, _ in bt.tuning(True)
+                       if "twide" in names})
     ms, by, kd = bt.profile(forward=True)
     bt.status()
     for i, (m, b, k) in enumerate(zip(ms, by, kd)):
@@ -891,7 +896,7 @@ def main():
     ap.add_argument("--probe-outputs", metavar="LEVELS:DIM:MODE",
                     help="time the restricted-output transform of one grid "
                          "(outputs: half the axis), e.g. 10,8,8:0:f64")
-    ap.add_argument("--probe-batch", metavar="LEVEL_SUM:MODE[:noslabs]",
+    ap.add_argument("--probe-batch", metavar="LEVEL_SUM:MODE[:noslabs][:tma]",
                     help="profile one direction of the 4D combination batch "
                          "at a smaller level sum launch by launch (for "
                          "kernel captures), e.g. 19:f32c")

@@ -330,14 +330,12 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
   job.log2_bx = std::min(std::min(lj.log2_inner, log2ct), 8);
   job.log2_sx = std::max(0, log2ct - lj.log2_inner);
   job.nxb = 1 << (log2ct - job.log2_bx - job.log2_sx);
-  job.log2_nbox = std::min(lj.log2_n, 8);
   tiles = (lj.columns + (1LL << (log2ct + log2u)) - 1) >> (log2ct + log2u);
   if (tiles >= (1LL << 30)) return false;
   long long const outer = lj.columns >> lj.log2_inner;
   if (log2G >= 3) {
     job.chunked = 1;
     job.nxb = 1;
-    job.log2_nbox = lj.log2_n;
     job.log2_bx = std::min(lj.log2_inner, log2ct);  // Bx >= 4: log2ct <= 6
     job.log2_sx = log2ct - job.log2_bx;
     cuuint64_t dims[5] = {4, static_cast<cuuint64_t>(1) << log2G,
@@ -363,7 +361,7 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
                         static_cast<cuuint64_t>(outer)};
   cuuint64_t strides[2] = {static_cast<cuuint64_t>(4) << lj.log2_kstride,
                            static_cast<cuuint64_t>(4) << lj.log2_astride};
-  cuuint32_t box[3] = {1u << job.log2_bx, 1u << job.log2_nbox,
+  cuuint32_t box[3] = {1u << job.log2_bx, 1u << lj.log2_n,
                        1u << job.log2_sx};
   cuuint32_t elem[3] = {1, 1, 1};
   CUresult const res = encode(

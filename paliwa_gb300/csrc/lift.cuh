@@ -215,13 +215,17 @@ __device__ __forceinline__ int tile_pitch(int G, int log2_inner,
 // one barrier per step (the same for every thread of the CTA: G is uniform
 // per tile). BAR = 0: the barrier is the CTA's; BAR > 0: named barrier BAR
 // among the NT threads that transform (a CTA whose other warps copy).
-// SHFL: the caller guarantees G <= 32 (the shared-memory paths compile out).
+// SHFL: the caller guarantees G <= 32 (the shared-memory paths compile out);
+// MAXG: the most chunks a pencil of the caller has (longer head pencils
+// compile out).
 __device__ __forceinline__ void named_barrier(int id, int count) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
 }
-template <class A, int NT, int BAR = 0, bool SHFL = false> struct RoundCtx {
+template <class A, int NT, int BAR = 0, bool SHFL = false, int MAXG = 256>
+struct RoundCtx {
   using V = typename A::V;
   static constexpr bool kShflOnly = SHFL;
+  static constexpr int kMaxG = MAXG;
   // Chunk heads of one column are consecutive threads (coarse_heads may
   // run a column's coarse levels as a pencil of heads in one warp).
   static constexpr bool kHeadPencil = true;
@@ -579,8 +583,14 @@ template <int W, bool FWD> struct WaveletSched {
         V *const col = ctx.heads + (w << ctx.log2G);
         switch (ctx.G) {
         case 64: head_pencil<2, A, NT>(col, lane, ctx.periodic, Lc); break;
-        case 128: head_pencil<4, A, NT>(col, lane, ctx.periodic, Lc); break;
-        case 256: head_pencil<8, A, NT>(col, lane, ctx.periodic, Lc); break;
+        case 128:
+          if constexpr (Ctx::kMaxG >= 128)
+            head_pencil<4, A, NT>(col, lane, ctx.periodic, Lc);
+          break;
+        case 256:
+          if constexpr (Ctx::kMaxG >= 256)
+            head_pencil<8, A, NT>(col, lane, ctx.periodic, Lc);
+          break;
         }
       }
       ctx.sync();

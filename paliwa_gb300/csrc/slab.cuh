@@ -149,6 +149,7 @@ template <class A, int NT> struct SlabCtx {
   using V = typename A::V;
   static constexpr bool kHeadPencil = false;
   static constexpr bool kShflOnly = false;
+  static constexpr int kMaxG = 256;
   __device__ __forceinline__ void sync() const { __syncthreads(); }
   int t, c, G, log2G, log2ls, gbase_lane, cbase;
   bool in_warp;

@@ -8,12 +8,10 @@
 // Ct = 2 NT / G consecutive columns (column = (outer index, inner index)) of
 // all n rows of their pencils. Each grid and axis has a 3D tensor map over
 // its [outer][n][inner] view (strides of the axis: sub-lattices included);
-// a tile is 1 or 2 column boxes {Bx columns of one outer index, Sx outer
-// indices} (Bx = min(inner, Ct, 256), Sx = Ct / inner when inner < Ct) of
-// n rows, in boxes of at most 256 rows (the tensor memory accelerator's
-// limit per box dimension), loaded into shared memory as
-// [column box][row box][outer][row][column], completion on an mbarrier with
-// a bounded wait. Every box starts on a 128-byte boundary of
+// a tile is 1 or 2 boxes {Bx columns of one outer index, n rows, Sx outer
+// indices} (Bx = min(inner, Ct, 256), Sx = Ct / inner when inner < Ct),
+// loaded into shared memory as [box][outer][row][column], completion on an
+// mbarrier with a bounded wait. Every box starts on a 128-byte boundary of
 // shared memory, as bulk tensor copies require; so the G chunks of a warp,
 // R rows apart, read the same banks (a G-way conflict on 8 or more chunks:
 // a pad after one box per chunk would remove it, but would move the boxes
@@ -62,8 +60,7 @@ struct TWideJob {
   int nlevels;
   int log2_bx;           // box: 2^log2_bx columns of one outer index
   int log2_sx;           // box: 2^log2_sx outer indices
-  int nxb;               // column boxes per tile
-  int log2_nbox;         // rows per box: min(n, 256)
+  int nxb;               // boxes per tile
   int chunked;           // 1: the chunk-interleaved layout (G >= 8)
 };
 
@@ -239,7 +236,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       z += xb << job.log2_sx;
   };
   auto box_bytes = [](TWideJob const &job) {
-    return 4 << (job.log2_bx + job.log2_nbox + job.log2_sx);
+    return 4 << (job.log2_bx + job.log2_n + job.log2_sx);
   };
 
   // The producer lane issues every copy; it keeps the last map it fenced.
@@ -255,22 +252,19 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       fenced = job.map;
     }
     int const bb = box_bytes(job);
-    int const nc = 1 << (job.log2_n - job.log2_nbox);  // row boxes
-    mbar_expect_tx(&full[b], static_cast<unsigned>(U * bb * job.nxb * nc));
+    mbar_expect_tx(&full[b], static_cast<unsigned>(U * bb * job.nxb));
     for (int u = 0; u < U; ++u) {
       int x0, z0;
       origin(job, tile, u, x0, z0);
       unsigned char *const dst = tiles + b * TILE + u * UNIT;
-      if (job.chunked) {  // one box: the unit (nxb = nc = 1)
+      if (job.chunked) {  // one box: the unit (nxb = 1)
         tma_load_5d(dst, map, x0 >> 2, z0, &full[b]);
         continue;
       }
       for (int xb = 0; xb < job.nxb; ++xb) {
         int x, z;
         box_at(job, xb, x0, z0, x, z);
-        for (int cb = 0; cb < nc; ++cb)
-          tma_load_3d(dst + (xb * nc + cb) * bb, map, x, cb << job.log2_nbox,
-                      z, &full[b]);
+        tma_load_3d(dst + xb * bb, map, x, 0, z, &full[b]);
       }
     }
   };
@@ -280,7 +274,6 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     TWideJob const &job = sjob[b];
     void const *const map = p.maps + job.map;
     int const bb = box_bytes(job);
-    int const nc = 1 << (job.log2_n - job.log2_nbox);
     for (int u = 0; u < U; ++u) {
       int x0, z0;
       origin(job, tile, u, x0, z0);
@@ -292,9 +285,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       for (int xb = 0; xb < job.nxb; ++xb) {
         int x, z;
         box_at(job, xb, x0, z0, x, z);
-        for (int cb = 0; cb < nc; ++cb)
-          tma_store_3d(map, x, cb << job.log2_nbox, z,
-                       src + (xb * nc + cb) * bb);
+        tma_store_3d(map, x, 0, z, src + xb * bb);
       }
     }
     bulk_commit();
@@ -361,7 +352,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     bool const valid =
         LONG ? (R == 16 && job.chunked && log2G >= 6 && log2G <= 7)
              : (static_cast<unsigned>(log2G) <= 5u &&
-                (!job.chunked || (R == 16 && log2G >= 3)));
+                (job.chunked ? R == 16 && log2G >= 3 : log2G <= 2));
     if (valid) {
       int const G = 1 << log2G;
       // Thread = (chunk c, column pair g). Up to 32 chunks: the chunks of a
@@ -390,15 +381,10 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
         int const rem = col & ((1 << log2bs) - 1);
         int const s = rem >> job.log2_bx;
         int const bcol = rem & ((1 << job.log2_bx) - 1);
-        // The box holding row c R of the thread's columns (its R rows lie
-        // in one box: 256 is a multiple of R), and that row in the box
-        int const r0 = c << LOG2R;
-        int const box = (xb << (job.log2_n - job.log2_nbox)) +
-                        (r0 >> job.log2_nbox);
-        int const jr = r0 & ((1 << job.log2_nbox) - 1);
-        // [box][outer][row][column]: rows are Bx apart
-        idx0 = (box << (log2bs + job.log2_nbox)) +
-               ((((s << job.log2_nbox) + jr) << job.log2_bx) + bcol);
+        // [box][outer][row][column]: row c R of the thread's columns; rows
+        // are Bx apart
+        idx0 = (xb << (log2bs + job.log2_n)) +
+               ((((s << job.log2_n) + (c << LOG2R)) << job.log2_bx) + bcol);
         log2rs = job.log2_bx;
       }
       for (int u = 0; u < U; ++u) {
@@ -409,7 +395,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
         for (int j = 0; j < R; ++j)
           v[j] = A::load(
               *reinterpret_cast<W const *>(tf + idx0 + (j << log2rs)));
-        RoundCtx<A, NT, 1, !LONG> ctx(t, c, G, log2G, lane, 1,
+        RoundCtx<A, NT, 1, !LONG, 128> ctx(t, c, G, log2G, lane, 1,
                                       LONG ? heads : nullptr,
                                       LONG ? xch : nullptr, log2ls);
         Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);

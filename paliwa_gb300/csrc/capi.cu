@@ -224,14 +224,6 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   // 8-byte copy pieces, and beyond 32 chunks the batch ran slower than on
   // the staged kernel); then the direct kernel, then the staged one.
   int const tile_log2G_max = v.wide_last ? 4 : v.log2_es == 3 ? 5 : 8;
-  // (The TMA wide kernel is the default for wide chunks of 8 and 16 points
-  // and for pencils of 8 to 32 chunks, where it measured faster per launch
-  // on the 4D CT batch: 4.73 against 4.01 TB/s at 8 points, 4.73 against
-  // 3.16 at 16, about 3.7 against 2.29 on the tile kernel's pencils of 128
-  // and 256 points, 0.46 against 0.71 ms on the staged kernel's pencils of
-  // 512; at 4 points the wide kernel is faster, 5.26 against 4.39-4.55
-  // TB/s, and on pencils of 1024 and 2048 points, whose chunks exchange
-  // through shared memory, the staged kernel: 2.2 against 2.6 TB/s.)
   if (k.has(kChooseWide) && (!last || v.wide_last))
     k.dflt = kChooseWide;
   else if (k.has(kChooseTile) && log2G <= tile_log2G_max)
@@ -241,8 +233,17 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   else
     k.dflt = staged_chunk(v) == 32 ? kChooseStaged32 : kChooseStaged;
   k.fallback = k.dflt;
+  // (The TMA wide kernel is the default for wide chunks of 8 and 16 points
+  // and for pencils of 8 to 128 chunks, measured on the 4D CT batch: per
+  // launch 4.73 against 4.01 TB/s at 8 points, 4.73 against 3.16 at 16,
+  // about 3.7 against 2.29 on the tile kernel's pencils of 128 and 256
+  // points, 0.46 against 0.71 ms on the staged kernel's pencils of 512; on
+  // pencils of 1024 and 2048 points, whose chunks exchange through shared
+  // memory, as fast as the staged kernel per launch (0.92 ms each) and the
+  // step 21.59 against 22.02 ms with it. At 4 points the wide kernel is
+  // faster, 5.26 against 4.39-4.55 TB/s.)
   if (k.has(kChooseTmaWide) &&
-      (wide_chunk(v.log2_n) >= 8 || (!k.has(kChooseWide) && log2G <= 5)))
+      (wide_chunk(v.log2_n) >= 8 || !k.has(kChooseWide)))
     k.dflt = kChooseTmaWide;
   return k;
 }

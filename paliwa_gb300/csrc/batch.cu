@@ -330,6 +330,7 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
   job.log2_bx = std::min(std::min(lj.log2_inner, log2ct), 8);
   job.log2_sx = std::max(0, log2ct - lj.log2_inner);
   job.nxb = 1 << (log2ct - job.log2_bx - job.log2_sx);
+  job.log2_rs = job.log2_bx;
   tiles = (lj.columns + (1LL << (log2ct + log2u)) - 1) >> (log2ct + log2u);
   if (tiles >= (1LL << 30)) return false;
   long long const outer = lj.columns >> lj.log2_inner;
@@ -338,6 +339,7 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
     job.nxb = 1;
     job.log2_bx = std::min(lj.log2_inner, log2ct);  // Bx >= 4: log2ct <= 6
     job.log2_sx = log2ct - job.log2_bx;
+    job.log2_rs = log2G + 2;
     cuuint64_t dims[5] = {4, static_cast<cuuint64_t>(1) << log2G,
                           static_cast<cuuint64_t>(r),
                           static_cast<cuuint64_t>(1) << (lj.log2_inner - 2),
@@ -461,10 +463,11 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
             int code = st.R;
             int const r = twide_chunk(st);
             if (tma && st.tma && r > 0 &&
-                canonical_shifts(st.job, (ws & 1) != 0))
+                canonical_shifts(st.job, (ws & 1) != 0)) {
+              int const log2G = st.job.log2_n - (31 - __builtin_clz(r));
               code = kTWide + r +
-                     (st.job.log2_n - (31 - __builtin_clz(r)) > 5 ? kTWideLong
-                                                                  : 0);
+                     (log2G > 5 ? kTWideLong : log2G >= 3 ? kTWideChunked : 0);
+            }
             by_r[code].push_back(&st);
           }
         for (auto const &[R, list] : by_r) {
@@ -481,7 +484,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
               TWideJob job;
               CUtensorMap map;
               long long tiles = 0;
-              if (!twide_job(*st, (R - kTWide) % kTWideLong, job, map,
+              if (!twide_job(*st, (R - kTWide) % kTWideChunked, job, map,
                              tiles)) {
                 rest[st->R].push_back(st);
                 continue;

@@ -48,8 +48,9 @@ namespace pgb {
 
 constexpr int kTWideThreads = 256;               // transform threads
 constexpr int kTWideBlock = kTWideThreads + 32;  // + the producer warp
-// Added to the chunk size of a launch whose pencils have more than 32
-// chunks (the LONG kernel).
+// Added to the chunk size of a launch whose pencils have 8 to 32 chunks
+// (chunked form) or more than 32 chunks (long form).
+constexpr int kTWideChunked = 32;
 constexpr int kTWideLong = 64;
 
 struct TWideJob {
@@ -62,6 +63,7 @@ struct TWideJob {
   int log2_sx;           // box: 2^log2_sx outer indices
   int nxb;               // boxes per tile
   int chunked;           // 1: the chunk-interleaved layout (G >= 8)
+  int log2_rs;           // floats between a thread's rows in shared memory
 };
 
 struct TWideParams {
@@ -169,14 +171,19 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
   return true;
 }
 
-// LONG: every job of the launch has pencils of 64 or 128 chunks (1024 and
-// 2048 points), held by consecutive threads, whose exchanges go through
-// shared memory under named barrier 1 among the NT transform threads (the
-// producer warp never takes part); otherwise pencils of at most 32 chunks,
-// exchanging by shuffles, and no barrier after the start.
-template <class A, int R, class Sched, bool LONG>
+// FORM (the same for every job of a launch): 0, pencils of up to 4 chunks in
+// the dense layout; 1, pencils of 8 to 32 chunks of 16 points in the
+// chunk-interleaved layout; 2 (long), pencils of 64 or 128 chunks (1024 and
+// 2048 points) in the chunk-interleaved layout, held by consecutive threads,
+// whose exchanges go through shared memory under named barrier 1 among the
+// NT transform threads (the producer warp never takes part). Forms 0 and 1
+// exchange by shuffles and have no barrier after the start. (One kernel for
+// forms 0 and 1 kept more registers live and spilled.)
+template <class A, int R, class Sched, int FORM>
 __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     twide_kernel(__grid_constant__ const TWideParams p) {
+  constexpr bool LONG = FORM == 2;
+  constexpr bool CHUNKED = FORM >= 1;
   using V = typename A::V;
   using W = typename A::Store;
   static_assert(sizeof(W) == 8, "rows of two float columns");
@@ -345,14 +352,15 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     }
     TWideJob const &job = sjob[b];
     int const log2G = job.log2_n - LOG2R;
-    // Jobs as the planner makes them: LONG launches 64 or 128 chunks of 16
-    // points in the chunked layout, the others at most 32 chunks (the
-    // exchange paths of longer pencils need the named barriers). The test
-    // is uniform over the tile, so every thread takes the same barriers.
+    // Jobs as the planner makes them for the launch's form (the exchange
+    // paths of pencils of more than 32 chunks need the named barriers of
+    // the long form). The test is uniform over the tile, so every thread
+    // takes the same barriers.
     bool const valid =
-        LONG ? (R == 16 && job.chunked && log2G >= 6 && log2G <= 7)
-             : (static_cast<unsigned>(log2G) <= 5u &&
-                (job.chunked ? R == 16 && log2G >= 3 : log2G <= 2));
+        (CHUNKED ? R == 16 && job.chunked &&
+                       log2G >= (LONG ? 6 : 3) && log2G <= (LONG ? 7 : 5)
+                 : !job.chunked && static_cast<unsigned>(log2G) <= 2u) &&
+        job.log2_rs == (CHUNKED ? log2G + 2 : job.log2_bx);
     if (valid) {
       int const G = 1 << log2G;
       // Thread = (chunk c, column pair g). Up to 32 chunks: the chunks of a
@@ -368,12 +376,13 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
         c = t & (G - 1);
         g = t >> log2G;
       }
-      // Float index of the thread's row j: idx0 + j * rstride.
-      int idx0, log2rs;
-      if (LONG || job.chunked) {
+      // Float index of the thread's row j: idx0 + (j << job.log2_rs) (the
+      // row stride read from the job in shared memory where needed: a
+      // register holding it through the transform made the kernel spill).
+      int idx0;
+      if constexpr (CHUNKED) {
         // [column quad][row of chunk][chunk][4 columns]
         idx0 = (((((g >> 1) << LOG2R) << log2G) + c) << 2) + 2 * (g & 1);
-        log2rs = log2G + 2;
       } else {
         int const col = 2 * g;
         int const log2bs = job.log2_bx + job.log2_sx;
@@ -385,7 +394,6 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
         // are Bx apart
         idx0 = (xb << (log2bs + job.log2_n)) +
                ((((s << job.log2_n) + (c << LOG2R)) << job.log2_bx) + bcol);
-        log2rs = job.log2_bx;
       }
       for (int u = 0; u < U; ++u) {
         float *const tf =
@@ -394,14 +402,15 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
 #pragma unroll
         for (int j = 0; j < R; ++j)
           v[j] = A::load(
-              *reinterpret_cast<W const *>(tf + idx0 + (j << log2rs)));
+              *reinterpret_cast<W const *>(tf + idx0 + (j << job.log2_rs)));
         RoundCtx<A, NT, 1, !LONG, 128> ctx(t, c, G, log2G, lane, 1,
                                       LONG ? heads : nullptr,
                                       LONG ? xch : nullptr, log2ls);
         Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
 #pragma unroll
         for (int j = 0; j < R; ++j)
-          *reinterpret_cast<W *>(tf + idx0 + (j << log2rs)) = A::store(v[j]);
+          *reinterpret_cast<W *>(tf + idx0 + (j << job.log2_rs)) =
+              A::store(v[j]);
       }
     } else if (lane == 0) {
       atomicExch(p.error, 1u);

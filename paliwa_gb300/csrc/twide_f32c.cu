@@ -7,11 +7,11 @@ namespace pgb {
 
 namespace {
 
-template <int R, class Sched, bool LONG>
+template <int R, class Sched, int FORM>
 void launch_twide_r(TWideParams const &p, cudaStream_t s) {
   static thread_local Occupancy occ;
-  auto kernel = twide_kernel<RowF32C, R, Sched, LONG>;
-  size_t const smem = twide_smem_bytes<R, LONG>();
+  auto kernel = twide_kernel<RowF32C, R, Sched, FORM>;
+  size_t const smem = twide_smem_bytes<R, FORM == 2>();
   int const dev = current_device();
   if (dev < 0 || dev >= Occupancy::kMaxDevices)
     throw StatusError(2, "device ordinal beyond the launch cache");
@@ -39,11 +39,12 @@ void launch_twide_r(TWideParams const &p, cudaStream_t s) {
 template <class Sched>
 void by_r(int R, TWideParams const &p, cudaStream_t s) {
   switch (R) {
-  case 2: return launch_twide_r<2, Sched, false>(p, s);
-  case 4: return launch_twide_r<4, Sched, false>(p, s);
-  case 8: return launch_twide_r<8, Sched, false>(p, s);
-  case 16: return launch_twide_r<16, Sched, false>(p, s);
-  case kTWideLong + 16: return launch_twide_r<16, Sched, true>(p, s);
+  case 2: return launch_twide_r<2, Sched, 0>(p, s);
+  case 4: return launch_twide_r<4, Sched, 0>(p, s);
+  case 8: return launch_twide_r<8, Sched, 0>(p, s);
+  case 16: return launch_twide_r<16, Sched, 0>(p, s);
+  case kTWideChunked + 16: return launch_twide_r<16, Sched, 1>(p, s);
+  case kTWideLong + 16: return launch_twide_r<16, Sched, 2>(p, s);
   }
   throw StatusError(2, "twide launch with an unsupported chunk size");
 }
@@ -51,7 +52,7 @@ void by_r(int R, TWideParams const &p, cudaStream_t s) {
 } // namespace
 
 // sched = 2 * wavelet + (forward ? 1 : 0); R = rows per chunk, plus
-// kTWideLong for pencils of more than 32 chunks.
+// kTWideChunked for pencils of 8 to 32 chunks and kTWideLong for more.
 void launch_twide_f32c(int sched, int R, TWideParams const &p,
                        cudaStream_t s) {
   switch (sched) {

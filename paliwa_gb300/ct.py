@@ -68,10 +68,12 @@ def packed_grids(levels, dtype, device="cuda", align=64):
     return buf, [buf.narrow(0, o, s) for o, s in zip(offsets, sizes)]
 
 
-# Launch codes of the slab kernel and (plus the chunk size, plus 64 for
-# pencils of more than 32 chunks) of the TMA wide kernel in Batch.profile.
+# Launch codes of the slab kernel and (plus the chunk size, plus 32 for
+# pencils of 8 to 32 chunks and 64 for more) of the TMA wide kernel in
+# Batch.profile.
 SLAB_KERNEL = 1024
 TWIDE_KERNEL = 2048
+TWIDE_CHUNKED = 32
 TWIDE_LONG = 64
 
 
@@ -79,6 +81,8 @@ def kernel_name(code):
     """Name of the lifting kernel behind a launch code of Batch.profile."""
     if code > TWIDE_KERNEL + TWIDE_LONG:
         return f"twide_kernel long R={code - TWIDE_KERNEL - TWIDE_LONG}"
+    if code > TWIDE_KERNEL + TWIDE_CHUNKED:
+        return f"twide_kernel chunked R={code - TWIDE_KERNEL - TWIDE_CHUNKED}"
     if code > TWIDE_KERNEL:
         return f"twide_kernel R={code - TWIDE_KERNEL}"
     if code == SLAB_KERNEL:

@@ -213,15 +213,10 @@ __device__ __forceinline__ int tile_pitch(int G, int log2_inner,
 // 2^log2ls apart (the wide kernel, whose neighbouring lanes hold
 // neighbouring columns). Longer columns exchange through shared memory with
 // one barrier per step (the same for every thread of the CTA: G is uniform
-// per tile). BAR = 0: the barrier is the CTA's; BAR > 0: named barrier BAR
-// among the NT threads that transform (a CTA whose other warps copy).
-// SHFL: the caller guarantees G <= 32 (the shared-memory paths compile out);
-// MAXG: the most chunks a pencil of the caller has (longer head pencils
-// compile out).
-__device__ __forceinline__ void named_barrier(int id, int count) {
-  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
-}
-template <class A, int NT, int BAR = 0, bool SHFL = false, int MAXG = 256>
+// per tile). SHFL: the caller guarantees G <= 32 (the shared-memory paths
+// compile out); MAXG: the most chunks a pencil of the caller has (longer
+// head pencils compile out).
+template <class A, int NT, bool SHFL = false, int MAXG = 256>
 struct RoundCtx {
   using V = typename A::V;
   static constexpr bool kShflOnly = SHFL;
@@ -244,12 +239,7 @@ struct RoundCtx {
   __device__ __forceinline__ int chunk_lane(int cc) const {
     return gbase_lane | ((cc & (G - 1)) << log2ls);
   }
-  __device__ __forceinline__ void sync() const {
-    if constexpr (BAR == 0)
-      __syncthreads();
-    else
-      named_barrier(BAR, NT);
-  }
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
 
   // The neighbour of a fine step: slot 0 of the next chunk (o = 1) or slot
   // R - s of the previous chunk (o = 0); `pub` is this chunk's value of it.

@@ -112,8 +112,8 @@ template <int R> struct TWideShape {
       size_t(kStages) * kTileBytes + 128;  // + 128-byte alignment slack
 };
 
-// Launches with pencils of more than 32 chunks also hold the exchange
-// buffers of their chunk heads (NT rows) and fine steps (2 NT rows).
+// The long form also holds the exchange buffers of its chunk heads (NT rows)
+// and fine steps (2 NT rows).
 template <int R, bool LONG> constexpr size_t twide_smem_bytes() {
   return TWideShape<R>::kSmemBytes + (LONG ? 3 * kTWideThreads * 16 : 0);
 }
@@ -136,21 +136,10 @@ __device__ __forceinline__ void tma_store_5d(void const *map, int q, int z,
       : "memory");
 }
 
-// True on every participating thread when `v` is true on all NT of them
-// (named barrier `id`).
-__device__ __forceinline__ bool named_barrier_and(int id, int count, bool v) {
-  unsigned r;
-  asm volatile(
-      "{\n"
-      ".reg .pred p, q;\n"
-      "setp.ne.u32 p, %1, 0;\n"
-      "bar.red.and.pred q, %2, %3, p;\n"
-      "selp.u32 %0, 1, 0, q;\n"
-      "}\n"
-      : "=r"(r)
-      : "r"(static_cast<unsigned>(v)), "r"(id), "r"(count)
-      : "memory");
-  return r != 0;
+// Waits until all but this thread's most recent bulk store group have read
+// their shared memory.
+__device__ __forceinline__ void bulk_wait_read_1() {
+  asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -173,17 +162,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
 
 // FORM (the same for every job of a launch): 0, pencils of up to 4 chunks in
 // the dense layout; 1, pencils of 8 to 32 chunks of 16 points in the
-// chunk-interleaved layout; 2 (long), pencils of 64 or 128 chunks (1024 and
-// 2048 points) in the chunk-interleaved layout, held by consecutive threads,
-// whose exchanges go through shared memory under named barrier 1 among the
-// NT transform threads (the producer warp never takes part). Forms 0 and 1
-// exchange by shuffles and have no barrier after the start. (One kernel for
-// forms 0 and 1 kept more registers live and spilled.)
+// chunk-interleaved layout. Both exchange by shuffles and have no barrier
+// after the start. (One kernel for both kept more registers live and
+// spilled.) Longer pencils: twide_long_kernel below.
 template <class A, int R, class Sched, int FORM>
 __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     twide_kernel(__grid_constant__ const TWideParams p) {
-  constexpr bool LONG = FORM == 2;
-  constexpr bool CHUNKED = FORM >= 1;
+  constexpr bool CHUNKED = FORM == 1;
   using V = typename A::V;
   using W = typename A::Store;
   static_assert(sizeof(W) == 8, "rows of two float columns");
@@ -198,8 +183,6 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
   unsigned const base_addr = smem_u32(smem_raw);
   unsigned char *const tiles =
       smem_raw + ((128 - (base_addr & 127)) & 127);  // 128-byte aligned
-  V *const heads = reinterpret_cast<V *>(tiles + S * TILE);  // LONG only
-  V *const xch = heads + NT;
   __shared__ uint64_t full[S], empty[S];
   __shared__ TWideJob sjob[S];
   __shared__ int abort_flag;  // set when a bounded wait gave up
@@ -336,14 +319,8 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     int const b = static_cast<int>(k % S);
     bool const ok = mbar_wait_bounded(
         &full[b], static_cast<unsigned>((k / S) & 1), abort);
-    // Threads that exchange leave together: a warp (shuffles), or with
-    // LONG all transform threads (named barriers).
-    bool all_ok;
-    if constexpr (LONG)
-      all_ok = named_barrier_and(1, NT, ok);
-    else
-      all_ok = __all_sync(0xffffffffu, ok);
-    if (!all_ok) {
+    // A warp leaves as a whole (its lanes exchange by shuffles).
+    if (!__all_sync(0xffffffffu, ok)) {
       if (lane == 0) {
         atomicExch(p.error, 1u);
         *abort = 1;
@@ -352,30 +329,19 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     }
     TWideJob const &job = sjob[b];
     int const log2G = job.log2_n - LOG2R;
-    // Jobs as the planner makes them for the launch's form (the exchange
-    // paths of pencils of more than 32 chunks need the named barriers of
-    // the long form). The test is uniform over the tile, so every thread
-    // takes the same barriers.
+    // Jobs as the planner makes them for the launch's form (pencils of
+    // more than 32 chunks would take exchange paths that need a barrier).
     bool const valid =
-        (CHUNKED ? R == 16 && job.chunked &&
-                       log2G >= (LONG ? 6 : 3) && log2G <= (LONG ? 7 : 5)
+        (CHUNKED ? R == 16 && job.chunked && log2G >= 3 && log2G <= 5
                  : !job.chunked && static_cast<unsigned>(log2G) <= 2u) &&
         job.log2_rs == (CHUNKED ? log2G + 2 : job.log2_bx);
     if (valid) {
       int const G = 1 << log2G;
-      // Thread = (chunk c, column pair g). Up to 32 chunks: the chunks of a
-      // column pair are lanes W = 32 / G apart, the W column pairs of one
-      // chunk consecutive; more: chunks in consecutive threads.
-      int c, g, log2ls;
-      if (!LONG) {
-        log2ls = 5 - log2G;
-        c = lane >> log2ls;
-        g = ((t >> 5) << log2ls) | (lane & ((1 << log2ls) - 1));
-      } else {
-        log2ls = 0;
-        c = t & (G - 1);
-        g = t >> log2G;
-      }
+      // Thread = (chunk c, column pair g): the chunks of a column pair are
+      // lanes W = 32 / G apart, the W column pairs of one chunk consecutive.
+      int const log2ls = 5 - log2G;
+      int const c = lane >> log2ls;
+      int const g = ((t >> 5) << log2ls) | (lane & ((1 << log2ls) - 1));
       // Float index of the thread's row j: idx0 + (j << job.log2_rs) (the
       // row stride read from the job in shared memory where needed: a
       // register holding it through the transform made the kernel spill).
@@ -403,9 +369,8 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
         for (int j = 0; j < R; ++j)
           v[j] = A::load(
               *reinterpret_cast<W const *>(tf + idx0 + (j << job.log2_rs)));
-        RoundCtx<A, NT, 1, !LONG, 128> ctx(t, c, G, log2G, lane, 1,
-                                      LONG ? heads : nullptr,
-                                      LONG ? xch : nullptr, log2ls);
+        RoundCtx<A, NT, true> ctx(t, c, G, log2G, lane, 1, nullptr, nullptr,
+                                  log2ls);
         Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
 #pragma unroll
         for (int j = 0; j < R; ++j)
@@ -418,6 +383,148 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     fence_proxy_async_smem();  // the writes above, before the tile's store
     mbar_arrive(&empty[b]);
   }
+}
+
+
+// Long form: periodic pencils of 64 or 128 chunks of 16 points (1024 and
+// 2048 points) in the chunk-interleaved layout. Their chunks are
+// consecutive threads and exchange through shared memory with a CTA barrier
+// per step, so every thread meets at barriers anyway: there is no producer
+// warp. Thread 0 issues the copies right after each tile's vote barrier
+// (every thread has then written the previous tile back): the store of tile
+// k - 1, and the load of tile k + 1 into the buffer of tile k - 2 once that
+// tile's store has read it. 256 threads per CTA leave 128 registers per
+// thread for two CTAs per SM (a producer warp would leave 96, and the form
+// spilled there).
+template <class A, class Sched>
+__global__ void __launch_bounds__(kTWideThreads, 2)
+    twide_long_kernel(__grid_constant__ const TWideParams p) {
+  using V = typename A::V;
+  using W = typename A::Store;
+  static_assert(sizeof(W) == 8, "rows of two float columns");
+  constexpr int R = 16;
+  constexpr int NT = kTWideThreads;
+  constexpr int S = TWideShape<R>::kStages;
+  static_assert(S == 3, "the copy order below assumes three tile buffers");
+  constexpr int TILE = TWideShape<R>::kTileBytes;
+  constexpr int LOG2R = Log2<R>::value;
+  constexpr int LOG2NT = Log2<NT>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned const base_addr = smem_u32(smem_raw);
+  unsigned char *const tiles =
+      smem_raw + ((128 - (base_addr & 127)) & 127);  // 128-byte aligned
+  V *const heads = reinterpret_cast<V *>(tiles + S * TILE);
+  V *const xch = heads + NT;
+  __shared__ uint64_t full[S];
+  __shared__ TWideJob sjob[S];
+
+  int const t = threadIdx.x;
+  int const lane = t & 31;
+  long long const first = blockIdx.x;
+  long long const step = gridDim.x;
+  if (first >= p.total_tiles) return;
+  long long const ntiles = (p.total_tiles - first + step - 1) / step;
+
+  if (t == 0) {
+    for (int b = 0; b < S; ++b) mbar_init(&full[b], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // Thread 0's copies (one 5D box per tile); it keeps the last map it
+  // fenced.
+  int fenced = -1;
+  auto origin = [](TWideJob const &job, long long tile, int &q0, int &z0) {
+    int const log2ct = LOG2NT + 1 - (job.log2_n - LOG2R);
+    long long const col0 = (tile - job.tile_begin) << log2ct;
+    z0 = static_cast<int>(col0 >> job.log2_inner);
+    q0 = static_cast<int>((col0 & ((1LL << job.log2_inner) - 1)) >> 2);
+  };
+  auto issue_load = [&](long long k) {
+    int const b = static_cast<int>(k % S);
+    long long const tile = first + k * step;
+    sjob[b] = p.jobs[p.tile_job[tile]];
+    TWideJob const &job = sjob[b];
+    void const *const map = p.maps + job.map;
+    if (job.map != fenced) {
+      fence_tensormap(map);
+      fenced = job.map;
+    }
+    mbar_expect_tx(&full[b], static_cast<unsigned>(TILE));
+    int q0, z0;
+    origin(job, tile, q0, z0);
+    tma_load_5d(tiles + b * TILE, map, q0, z0, &full[b]);
+  };
+  auto issue_store = [&](long long k) {
+    int const b = static_cast<int>(k % S);
+    long long const tile = first + k * step;
+    TWideJob const &job = sjob[b];
+    int q0, z0;
+    origin(job, tile, q0, z0);
+    tma_store_5d(p.maps + job.map, q0, z0, tiles + b * TILE);
+    bulk_commit();
+  };
+
+  if (t == 0) issue_load(0);
+  long long k = 0;
+  for (; k < ntiles; ++k) {
+    int const b = static_cast<int>(k % S);
+    // Bounded wait for tile k, then a vote so that every thread leaves
+    // together if one gave up (no barrier is left waiting).
+    bool done = false;
+    long long const t0 = clock64();
+    while (!(done = mbar_try_wait(&full[b],
+                                  static_cast<unsigned>((k / S) & 1))))
+      if (clock64() - t0 > (1LL << 31)) break;
+    if (!__syncthreads_and(done)) break;
+    if (t == 0) {
+      if (k >= 1) issue_store(k - 1);  // its writes are in (the barrier)
+      if (k + 1 < ntiles) {
+        bulk_wait_read_1();  // the store of tile k - 2 has read its buffer
+        issue_load(k + 1);
+      }
+    }
+    TWideJob const &job = sjob[b];
+    int const log2G = job.log2_n - LOG2R;
+    // Jobs as the planner makes them (uniform over the tile, so every
+    // thread takes the same barriers).
+    if (job.chunked && log2G >= 6 && log2G <= 7 && job.log2_rs == log2G + 2) {
+      int const G = 1 << log2G;
+      // Thread = (chunk c, column pair g): chunks in consecutive threads.
+      int const c = t & (G - 1);
+      int const g = t >> log2G;
+      // [column quad][row of chunk][chunk][4 columns]
+      int const idx0 =
+          (((((g >> 1) << LOG2R) << log2G) + c) << 2) + 2 * (g & 1);
+      float *const tf = reinterpret_cast<float *>(tiles + b * TILE);
+      V v[R];
+#pragma unroll
+      for (int j = 0; j < R; ++j)
+        v[j] = A::load(
+            *reinterpret_cast<W const *>(tf + idx0 + (j << job.log2_rs)));
+      RoundCtx<A, NT, false, 128> ctx(t, c, G, log2G, lane, 1, heads, xch);
+      Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
+#pragma unroll
+      for (int j = 0; j < R; ++j)
+        *reinterpret_cast<W *>(tf + idx0 + (j << job.log2_rs)) =
+            A::store(v[j]);
+    } else if (t == 0) {
+      atomicExch(p.error, 1u);
+    }
+    fence_proxy_async_smem();  // the writes above, before the tile's store
+  }
+  if (k == ntiles) {
+    __syncthreads();  // every thread has written the last tile back
+    if (t == 0) issue_store(k - 1);
+  } else if (t == 0) {
+    atomicExch(p.error, 1u);
+    // Tile k's load (the only one in flight) must end before the CTA's
+    // shared memory goes away.
+    long long const t0 = clock64();
+    while (!mbar_try_wait(&full[k % S], static_cast<unsigned>((k / S) & 1)))
+      if (clock64() - t0 > (1LL << 31)) break;
+  }
+  if (t == 0) bulk_wait_all();
 }
 
 } // namespace pgb

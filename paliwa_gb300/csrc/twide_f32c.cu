@@ -10,8 +10,15 @@ namespace {
 template <int R, class Sched, int FORM>
 void launch_twide_r(TWideParams const &p, cudaStream_t s) {
   static thread_local Occupancy occ;
-  auto kernel = twide_kernel<RowF32C, R, Sched, FORM>;
-  size_t const smem = twide_smem_bytes<R, FORM == 2>();
+  constexpr bool kLong = FORM == 2;
+  constexpr int kBlock = kLong ? kTWideThreads : kTWideBlock;
+  auto kernel = [] {
+    if constexpr (kLong)
+      return twide_long_kernel<RowF32C, Sched>;
+    else
+      return twide_kernel<RowF32C, R, Sched, FORM>;
+  }();
+  size_t const smem = twide_smem_bytes<R, kLong>();
   int const dev = current_device();
   if (dev < 0 || dev >= Occupancy::kMaxDevices)
     throw StatusError(2, "device ordinal beyond the launch cache");
@@ -24,7 +31,7 @@ void launch_twide_r(TWideParams const &p, cudaStream_t s) {
                "cudaFuncSetAttribute(twide)");
     int n = 0;
     cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &n, kernel, kTWideBlock, smem),
+                   &n, kernel, kBlock, smem),
                "occupancy query (twide)");
     sms = device_sms();
     per_sm = n < 1 ? 1 : n;
@@ -32,7 +39,7 @@ void launch_twide_r(TWideParams const &p, cudaStream_t s) {
   long long const resident =
       static_cast<long long>(capped_per_sm(per_sm, p.ctas_per_sm)) * sms;
   long long const blocks = std::min(p.total_tiles, resident);
-  kernel<<<static_cast<unsigned>(blocks), kTWideBlock, smem, s>>>(p);
+  kernel<<<static_cast<unsigned>(blocks), kBlock, smem, s>>>(p);
   cuda_check(cudaGetLastError(), "twide kernel launch");
 }
 

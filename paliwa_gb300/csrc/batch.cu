@@ -294,6 +294,8 @@ int twide_chunk(Stage const &st) {
   int const R = st.R;
   if (R == kWide + 2 || R == kWide + 4 || R == kWide + 8 || R == kWide + 16)
     return R - kWide;
+  if (R == kWideContig + 4 || R == kWideContig + 8 || R == kWideContig + 16)
+    return R - kWideContig;
   if ((R == kTile + 16 || R == kTileLong + 16 || R == 16 || R == 32) &&
       st.job.log2_n >= 7 && st.job.log2_n <= 11)
     return 16;
@@ -315,8 +317,38 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
   LiftJob const &lj = st.job;
   int const log2r = 31 - __builtin_clz(static_cast<unsigned>(r));
   int const log2G = lj.log2_n - log2r;
-  if (encode == nullptr || lj.periodic != 1 || lj.base % 16 != 0 ||
-      lj.log2_inner < 2 || log2G < 0 || log2G > 7 || lj.log2_n > 11 ||
+  if (encode == nullptr || lj.periodic != 1 || lj.base % 16 != 0)
+    return false;
+  if (lj.log2_inner == 0 && lj.log2_kstride == 0) {
+    // The last axis (contiguous layout): the grid as rows of 32 floats (128
+    // bytes), boxes of the unit's 16 r rows, 128-byte swizzle; units of
+    // 512 r floats (whole pencils).
+    if (r < 4 || log2G < 0 || log2G > 5) return false;
+    long long const points = lj.columns << lj.log2_n;
+    int const log2unit = 9 + log2r;
+    int const log2u = r >= 8 ? 0 : 3 - log2r;  // units per tile
+    if (points % 32 != 0 || (points >> (log2unit + log2u)) >= (1LL << 30))
+      return false;
+    tiles = (points + (1LL << (log2unit + log2u)) - 1) >> (log2unit + log2u);
+    std::memset(&job, 0, sizeof(job));
+    job.log2_n = lj.log2_n;
+    job.nlevels = lj.nlevels;
+    job.chunked = 2;
+    job.nxb = 1;
+    job.log2_bx = log2unit - lj.log2_n;  // box bytes = the unit
+    job.log2_sx = 0;
+    cuuint64_t dims[2] = {32, static_cast<cuuint64_t>(points / 32)};
+    cuuint64_t strides[1] = {128};
+    cuuint32_t box[2] = {32, static_cast<cuuint32_t>(16 * r)};
+    cuuint32_t elem[2] = {1, 1};
+    CUresult const res = encode(
+        &map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+        reinterpret_cast<void *>(lj.base), dims, strides, box, elem,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return res == CUDA_SUCCESS;
+  }
+  if (lj.log2_inner < 2 || log2G < 0 || log2G > 7 || lj.log2_n > 11 ||
       (log2G > 2 && r != 16))
     return false;
   int const log2ct = Log2<kTWideThreads>::value + 1 - log2G;
@@ -465,8 +497,12 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
             if (tma && st.tma && r > 0 &&
                 canonical_shifts(st.job, (ws & 1) != 0)) {
               int const log2G = st.job.log2_n - (31 - __builtin_clz(r));
+              bool const last =
+                  st.job.log2_inner == 0 && st.job.log2_kstride == 0;
               code = kTWide + r +
-                     (log2G > 5 ? kTWideLong : log2G >= 3 ? kTWideChunked : 0);
+                     (last ? kTWideContig
+                           : log2G > 5 ? kTWideLong
+                                       : log2G >= 3 ? kTWideChunked : 0);
             }
             by_r[code].push_back(&st);
           }

@@ -215,6 +215,10 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
                              wide_chunk(v.log2_n)))) <= 2) ||
        (R == 16 && log2G >= 3 && log2G <= 7)))
     k.mask |= 1 << kChooseTmaWide;
+  // ... and the last axis' wide stages of chunks of 4 to 16 points.
+  if (last && v.wide_last && k.has(kChooseWide) && R >= 4 &&
+      v.base % 16 == 0)
+    k.mask |= 1 << kChooseTmaWide;
   // Default: the wide kernel for strided pencils (and FP32c last-axis
   // pencils: measured on 2^26-point grids, 3.0-4.5 TB/s against 2.8-4.1 on
   // the direct kernel), then the tile kernel up to the length where it was
@@ -233,17 +237,20 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   else
     k.dflt = staged_chunk(v) == 32 ? kChooseStaged32 : kChooseStaged;
   k.fallback = k.dflt;
-  // (The TMA wide kernel is the default for wide chunks of 8 and 16 points
-  // and for pencils of 8 to 128 chunks, measured on the 4D CT batch: per
-  // launch 4.73 against 4.01 TB/s at 8 points, 4.73 against 3.16 at 16,
-  // about 3.7 against 2.29 on the tile kernel's pencils of 128 and 256
-  // points, 0.46 against 0.71 ms on the staged kernel's pencils of 512; on
-  // pencils of 1024 and 2048 points, whose chunks exchange through shared
-  // memory, as fast as the staged kernel per launch (0.92 ms each) and the
-  // step 21.59 against 22.02 ms with it. At 4 points the wide kernel is
-  // faster, 5.26 against 4.39-4.55 TB/s.)
+  // (The TMA wide kernel is the default for strided wide chunks of 8 and
+  // 16 points, for strided pencils of 8 to 128 chunks and for the last
+  // axis' wide stages, measured on the 4D CT batch: per launch 4.73 against
+  // 4.01 TB/s at 8 points, 4.73 against 3.16 at 16, about 3.7 against 2.29
+  // on the tile kernel's pencils of 128 and 256 points, 0.46 against 0.71
+  // ms on the staged kernel's pencils of 512; on pencils of 1024 and 2048
+  // points, whose chunks exchange through shared memory, as fast as the
+  // staged kernel per launch (0.92 ms each) and the step 21.59 against
+  // 22.02 ms with it; on the last axis 4.86 against 3.60 TB/s at 16 points,
+  // 4.97 against 4.42 at 8 and 4.96 against 4.79 at 4 (the step 20.37
+  // against 21.20 ms). On strided 4-point chunks the wide kernel is faster,
+  // 5.26 against 4.39-4.55 TB/s.)
   if (k.has(kChooseTmaWide) &&
-      (wide_chunk(v.log2_n) >= 8 || !k.has(kChooseWide)))
+      (last || wide_chunk(v.log2_n) >= 8 || !k.has(kChooseWide)))
     k.dflt = kChooseTmaWide;
   return k;
 }

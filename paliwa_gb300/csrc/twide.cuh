@@ -49,9 +49,11 @@ namespace pgb {
 constexpr int kTWideThreads = 256;               // transform threads
 constexpr int kTWideBlock = kTWideThreads + 32;  // + the producer warp
 // Added to the chunk size of a launch whose pencils have 8 to 32 chunks
-// (chunked form) or more than 32 chunks (long form).
+// (chunked form), more than 32 chunks (long form), or lie along the last
+// axis (contiguous form).
 constexpr int kTWideChunked = 32;
 constexpr int kTWideLong = 64;
+constexpr int kTWideContig = 96;
 
 struct TWideJob {
   long long tile_begin;  // first tile of this job in the launch
@@ -62,7 +64,8 @@ struct TWideJob {
   int log2_bx;           // box: 2^log2_bx columns of one outer index
   int log2_sx;           // box: 2^log2_sx outer indices
   int nxb;               // boxes per tile
-  int chunked;           // 1: the chunk-interleaved layout (G >= 8)
+  int chunked;           // 1: the chunk-interleaved layout (G >= 8),
+                         // 2: the contiguous layout (the last axis)
   int log2_rs;           // floats between a thread's rows in shared memory
 };
 
@@ -109,7 +112,7 @@ template <int R> struct TWideShape {
   static constexpr int kTileBytes = kUnits * kUnitBytes;
   static constexpr int kStages = R >= 16 ? 3 : 4;
   static constexpr size_t kSmemBytes =
-      size_t(kStages) * kTileBytes + 128;  // + 128-byte alignment slack
+      size_t(kStages) * kTileBytes + 1024;  // + 1024-byte alignment slack
 };
 
 // The long form also holds the exchange buffers of its chunk heads (NT rows)
@@ -162,13 +165,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
 
 // FORM (the same for every job of a launch): 0, pencils of up to 4 chunks in
 // the dense layout; 1, pencils of 8 to 32 chunks of 16 points in the
-// chunk-interleaved layout. Both exchange by shuffles and have no barrier
-// after the start. (One kernel for both kept more registers live and
+// chunk-interleaved layout; 3, last-axis pencils of up to 32 chunks of 4, 8
+// or 16 points in the contiguous layout: a unit is 2 NT R consecutive
+// floats (whole pencils), moved as 128-byte rows of a 2D tensor map with
+// the 128-byte swizzle (16-byte piece q of row r stored at q ^ (r mod 8)),
+// so that the lanes of a warp, each reading 16-byte pieces of its own
+// pencils' rows, fall on different banks (at most two lanes per bank
+// group). All forms exchange by shuffles and have no barrier after the
+// start. (One kernel for several forms kept more registers live and
 // spilled.) Longer pencils: twide_long_kernel below.
 template <class A, int R, class Sched, int FORM>
 __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     twide_kernel(__grid_constant__ const TWideParams p) {
   constexpr bool CHUNKED = FORM == 1;
+  constexpr bool CONTIG = FORM == 3;
   using V = typename A::V;
   using W = typename A::Store;
   static_assert(sizeof(W) == 8, "rows of two float columns");
@@ -182,7 +192,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned const base_addr = smem_u32(smem_raw);
   unsigned char *const tiles =
-      smem_raw + ((128 - (base_addr & 127)) & 127);  // 128-byte aligned
+      smem_raw + ((1024 - (base_addr & 1023)) & 1023);  // swizzle atoms
   __shared__ uint64_t full[S], empty[S];
   __shared__ TWideJob sjob[S];
   __shared__ int abort_flag;  // set when a bounded wait gave up
@@ -228,6 +238,11 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
   auto box_bytes = [](TWideJob const &job) {
     return 4 << (job.log2_bx + job.log2_n + job.log2_sx);
   };
+  // Contiguous layout: the first 128-byte row of unit u of `tile` (a unit
+  // is 16 R rows).
+  auto contig_row = [](TWideJob const &job, long long tile, int u) {
+    return static_cast<int>(((tile - job.tile_begin) * U + u) << (LOG2R + 4));
+  };
 
   // The producer lane issues every copy; it keeps the last map it fenced.
   int fenced = -1;
@@ -247,6 +262,11 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       int x0, z0;
       origin(job, tile, u, x0, z0);
       unsigned char *const dst = tiles + b * TILE + u * UNIT;
+      if constexpr (CONTIG) {  // one box of 16 R rows of 128 bytes
+        tma_load_2d(dst, reinterpret_cast<CUtensorMap const *>(map), 0,
+                    contig_row(job, tile, u), &full[b]);
+        continue;
+      }
       if (job.chunked) {  // one box: the unit (nxb = 1)
         tma_load_5d(dst, map, x0 >> 2, z0, &full[b]);
         continue;
@@ -268,6 +288,11 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       int x0, z0;
       origin(job, tile, u, x0, z0);
       unsigned char const *const src = tiles + b * TILE + u * UNIT;
+      if constexpr (CONTIG) {
+        tma_store_2d(reinterpret_cast<CUtensorMap const *>(map), 0,
+                     contig_row(job, tile, u), src);
+        continue;
+      }
       if (job.chunked) {
         tma_store_5d(map, x0 >> 2, z0, src);
         continue;
@@ -332,10 +357,58 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     // Jobs as the planner makes them for the launch's form (pencils of
     // more than 32 chunks would take exchange paths that need a barrier).
     bool const valid =
-        (CHUNKED ? R == 16 && job.chunked && log2G >= 3 && log2G <= 5
-                 : !job.chunked && static_cast<unsigned>(log2G) <= 2u) &&
-        job.log2_rs == (CHUNKED ? log2G + 2 : job.log2_bx);
-    if (valid) {
+        CONTIG ? R >= 4 && job.chunked == 2 &&
+                     static_cast<unsigned>(log2G) <= 5u
+               : (CHUNKED ? R == 16 && job.chunked == 1 && log2G >= 3 &&
+                                log2G <= 5
+                          : !job.chunked &&
+                                static_cast<unsigned>(log2G) <= 2u) &&
+                     job.log2_rs == (CHUNKED ? log2G + 2 : job.log2_bx);
+    if constexpr (CONTIG) {
+      if (valid) {
+        // Thread = (chunk c, column pair g): the G chunks of a pencil pair
+        // are consecutive lanes; column e of the pair is pencil 2 g + e,
+        // whose chunk starts at float (2 g + e) n + c R of the unit.
+        int const c = lane & ((1 << log2G) - 1);
+        int const g = t >> log2G;
+        // The byte offset of piece i of column e: rows of 128 bytes, pieces
+        // of 16 bytes swizzled within their row.
+        auto piece = [&](int e, int i) {
+          int const o = ((2 * g + e) << job.log2_n) + (c << LOG2R);
+          int const row = o >> 5;
+          return (row << 7) + (((((o & 31) >> 2) + i) ^ (row & 7)) << 4);
+        };
+        for (int u = 0; u < U; ++u) {
+          unsigned char *const ub = tiles + b * TILE + u * UNIT;
+          V v[R];
+#pragma unroll
+          for (int i = 0; i < R / 4; ++i) {
+            uint4 const f0 = *reinterpret_cast<uint4 const *>(ub + piece(0, i));
+            uint4 const f1 = *reinterpret_cast<uint4 const *>(ub + piece(1, i));
+            v[4 * i] = A::load(W{f0.x, f1.x});
+            v[4 * i + 1] = A::load(W{f0.y, f1.y});
+            v[4 * i + 2] = A::load(W{f0.z, f1.z});
+            v[4 * i + 3] = A::load(W{f0.w, f1.w});
+          }
+          RoundCtx<A, NT, true> ctx(t, c, 1 << log2G, log2G, lane, 1,
+                                    nullptr, nullptr);
+          Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
+#pragma unroll
+          for (int i = 0; i < R / 4; ++i) {
+            W const r0 = A::store(v[4 * i]);
+            W const r1 = A::store(v[4 * i + 1]);
+            W const r2 = A::store(v[4 * i + 2]);
+            W const r3 = A::store(v[4 * i + 3]);
+            *reinterpret_cast<uint4 *>(ub + piece(0, i)) =
+                uint4{r0.x, r1.x, r2.x, r3.x};
+            *reinterpret_cast<uint4 *>(ub + piece(1, i)) =
+                uint4{r0.y, r1.y, r2.y, r3.y};
+          }
+        }
+      } else if (lane == 0) {
+        atomicExch(p.error, 1u);
+      }
+    } else if (valid) {
       int const G = 1 << log2G;
       // Thread = (chunk c, column pair g): the chunks of a column pair are
       // lanes W = 32 / G apart, the W column pairs of one chunk consecutive.

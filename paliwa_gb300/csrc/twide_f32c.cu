@@ -51,6 +51,9 @@ void by_r(int R, TWideParams const &p, cudaStream_t s) {
   case 8: return launch_twide_r<8, Sched, 0>(p, s);
   case 16: return launch_twide_r<16, Sched, 0>(p, s);
   case kTWideChunked + 16: return launch_twide_r<16, Sched, 1>(p, s);
+  case kTWideContig + 4: return launch_twide_r<4, Sched, 3>(p, s);
+  case kTWideContig + 8: return launch_twide_r<8, Sched, 3>(p, s);
+  case kTWideContig + 16: return launch_twide_r<16, Sched, 3>(p, s);
   case kTWideLong + 16: return launch_twide_r<16, Sched, 2>(p, s);
   }
   throw StatusError(2, "twide launch with an unsupported chunk size");
@@ -59,7 +62,8 @@ void by_r(int R, TWideParams const &p, cudaStream_t s) {
 } // namespace
 
 // sched = 2 * wavelet + (forward ? 1 : 0); R = rows per chunk, plus
-// kTWideChunked for pencils of 8 to 32 chunks and kTWideLong for more.
+// kTWideChunked for pencils of 8 to 32 chunks, kTWideLong for more, and
+// kTWideContig for the last axis.
 void launch_twide_f32c(int sched, int R, TWideParams const &p,
                        cudaStream_t s) {
   switch (sched) {

@@ -69,16 +69,20 @@ def packed_grids(levels, dtype, device="cuda", align=64):
 
 
 # Launch codes of the slab kernel and (plus the chunk size, plus 32 for
-# pencils of 8 to 32 chunks and 64 for more) of the TMA wide kernel in
-# Batch.profile.
+# pencils of 8 to 32 chunks, 64 for more and 96 for the last axis) of the
+# TMA wide kernel in Batch.profile.
 SLAB_KERNEL = 1024
 TWIDE_KERNEL = 2048
 TWIDE_CHUNKED = 32
 TWIDE_LONG = 64
+TWIDE_CONTIG = 96
 
 
 def kernel_name(code):
     """Name of the lifting kernel behind a launch code of Batch.profile."""
+    if code > TWIDE_KERNEL + TWIDE_CONTIG:
+        return ("twide_kernel last axis "
+                f"R={code - TWIDE_KERNEL - TWIDE_CONTIG}")
     if code > TWIDE_KERNEL + TWIDE_LONG:
         return f"twide_kernel long R={code - TWIDE_KERNEL - TWIDE_LONG}"
     if code > TWIDE_KERNEL + TWIDE_CHUNKED:

@@ -505,7 +505,7 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
     rng = np.random.default_rng(78)
     host = [rng.uniform(-1, 1, 1 << sum(l)).astype(np.float32)
             for l in levels]
-    seen = set()
+    seen, seen_last = set(), set()
     for wavelet in ("hat", "biorthogonal", "fullweighting"):
         out = []
         for kernel in ("twide", "other"):
@@ -528,6 +528,9 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
                 if kernel == "twide":
                     seen.update(d["log2_n"] for c, d, _, _ in
                                 b.tuning(forward) if c in cls)
+                    seen_last.update(d["log2_n"] for c, d, _, _ in
+                                     b.tuning(forward)
+                                     if c in cls and d["last"])
             s = torch.cuda.Stream()
             kernels = b.profile(True, stream=s)[2]
             assert any(k > pct.TWIDE_KERNEL for k in kernels) == \
@@ -553,5 +556,7 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
             b.close()
         assert torch.equal(out[0][0], out[1][0]), wavelet
         assert torch.equal(out[0][1], out[1][1]), wavelet
-    # pencils of 4 to 2048 points (axes at level 1 = lmin have nothing to do)
+    # pencils of 4 to 2048 points (axes at level 1 = lmin have nothing to
+    # do), strided and along the last axis
     assert {2, 3, 4, 5, 6, 7, 8, 9, 10, 11} <= seen, seen
+    assert {2, 3, 4, 5, 6} <= seen_last, seen_last

@@ -255,18 +255,17 @@ int paliwa_gb_batch_set_groups(paliwa_gb_batch *batch, int ngroups);
  * directions after synchronizing the device. No counterpart in the
  * reference. */
 int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable);
-/* enable != 0 (default): FP32-compensated strided stages of up to 16
- * chunks per pencil (the wide kernel's pencils of up to 64 points and the
- * tile kernel's of 128 and 256; inner extent of 4 or more columns, 16-byte
- * aligned grids) may run on the TMA wide kernel: the wide kernel's register
- * transform, with each tile of columns moved between HBM and shared memory
- * by bulk tensor copies over a tensor map of the grid's axis (bounded
- * waits, reported by paliwa_gb_batch_status). It is the planner's default
- * for wide chunks of 8 and 16 points and for pencils of 128 and 256 points,
- * and an autotuner choice for the others. 0 keeps every such stage on the
- * wide or tile kernel's per-thread copies. Results are the same bits either
- * way. Re-plans both directions after synchronizing the device. No
- * counterpart in the reference. */
+/* enable != 0 (default): FP32-compensated stages of strided pencils of up
+ * to 2048 points (up to 128 chunks; inner extent of 4 or more columns) and
+ * of the last axis' pencils of up to 512 points, in 16-byte aligned grids,
+ * may run on the TMA wide kernel: the wide kernel's register transform,
+ * with each tile moved between HBM and shared memory by bulk tensor copies
+ * over a tensor map of the grid's axis (bounded waits, reported by
+ * paliwa_gb_batch_status). It is the planner's default for them except the
+ * strided 4-point chunks, which stay an autotuner choice. 0 keeps every
+ * such stage on the wide, tile or staged kernel's per-thread copies.
+ * Results are the same bits either way. Re-plans both directions after
+ * synchronizing the device. No counterpart in the reference. */
 int paliwa_gb_batch_use_tma(paliwa_gb_batch *batch, int enable);
 /* ctas > 0 caps every launch of the batch at that many CTAs per SM (the
  * kernels are persistent: by default a launch takes every slot that fits),
@@ -293,7 +292,8 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
  * (its bytes count one read and one write of each point it copies), 1024
  * the slab kernel (every level of a grid's
  * trailing axes in one pass; its bytes count one read and one write of each
- * point), 2048 + R the TMA wide kernel; `kernels` may be null. Call with
+ * point), 2048 + R the TMA wide kernel (+ 32: pencils of 8 to 32 chunks,
+ * + 64: more, + 96: the last axis); `kernels` may be null. Call with
  * capacity 0 to get *nlaunches first. */
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,

@@ -1,29 +1,36 @@
 // TMA wide kernel: the wide kernel's register transform (rows of two
 // adjacent columns as double-float f32x2 pairs, chunks of one pencil in
-// lanes 32 / G apart, shuffles only) for strided axes with pencils of up to
-// 512 points (G <= 32 chunks), with the data moved by the tensor memory
-// accelerator instead of per-thread copies.
+// lanes, shuffles) for strided pencils of up to 2048 points (G <= 128
+// chunks) and the last axis' pencils of up to 512 points, with the data
+// moved by the tensor memory accelerator instead of per-thread copies.
 //
-// A tile is one unit of the wide kernel: NT threads x R rows x 2 columns =
-// Ct = 2 NT / G consecutive columns (column = (outer index, inner index)) of
-// all n rows of their pencils. Each grid and axis has a 3D tensor map over
-// its [outer][n][inner] view (strides of the axis: sub-lattices included);
-// a tile is 1 or 2 boxes {Bx columns of one outer index, n rows, Sx outer
-// indices} (Bx = min(inner, Ct, 256), Sx = Ct / inner when inner < Ct),
-// loaded into shared memory as [box][outer][row][column], completion on an
-// mbarrier with a bounded wait. Every box starts on a 128-byte boundary of
-// shared memory, as bulk tensor copies require; so the G chunks of a warp,
-// R rows apart, read the same banks (a G-way conflict on 8 or more chunks:
-// a pad after one box per chunk would remove it, but would move the boxes
-// off the 128-byte boundaries). After the transform the threads write
-// their rows back into the same place and one thread stores the boxes with
-// bulk tensor stores. Columns past the end of the grid are read as zeros and not
-// stored (the tensor map's bounds). The copies are asynchronous and issued
-// by one thread, which removes the per-thread copy instructions that
-// throttled the wide kernel's memory pipeline (measured on a copy-only
-// build: MIO throttle of 10 per issue).
+// A tile is one unit of the wide kernel (several for chunks of up to 8
+// points): NT threads x R rows x 2 columns = Ct = 2 NT / G consecutive
+// columns (column = (outer index, inner index)) of all n rows of their
+// pencils. Each grid and axis has a tensor map, in one of three layouts:
+//  * dense (up to 4 chunks): a 3D map over the [outer][n][inner] view
+//    (strides of the axis: sub-lattices included); a tile is 1 or 2 boxes
+//    {Bx columns of one outer index, n rows, Sx outer indices} (Bx =
+//    min(inner, Ct, 256), Sx = Ct / inner when inner < Ct), in shared
+//    memory as [box][outer][row][column];
+//  * chunk-interleaved (8 to 128 chunks of 16 points): a 5D map {4 columns,
+//    G chunks, R rows of a chunk, column quads, outer index} and one box per
+//    tile, in shared memory as [column quad][row of chunk][chunk][4
+//    columns], so that the chunks a warp reads together lie in consecutive
+//    16-byte groups (with the dense layout they would read rows R apart, on
+//    the same banks; a pad after a box per chunk is not possible, since
+//    bulk tensor copies need 128-byte aligned shared-memory destinations);
+//  * contiguous (the last axis): see FORM 3 of twide_kernel.
+// Completion is on an mbarrier with a bounded wait. After the transform the
+// threads write their rows back into the same place and one thread stores
+// the boxes with bulk tensor stores. Columns past the end of the grid are
+// read as zeros and not stored (the tensor map's bounds). The copies are
+// asynchronous and issued by one thread, which removes the per-thread copy
+// instructions that throttled the wide kernel's memory pipeline (measured
+// on a copy-only build: MIO throttle of 10 per issue).
 //
-// The CTA is warp-specialised: NT transform threads (eight warps) and one
+// twide_kernel's CTA is warp-specialised: NT transform threads (eight
+// warps) and one
 // producer warp, of which one lane issues every copy. S tile buffers cycle
 // through two mbarriers each: `full` (the tile's loads have landed; the
 // producer arrives with the byte count) and `empty` (all NT transform

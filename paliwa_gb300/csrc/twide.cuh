@@ -30,9 +30,8 @@
 // on a copy-only build: MIO throttle of 10 per issue).
 //
 // twide_kernel's CTA is warp-specialised: NT transform threads (eight
-// warps) and one
-// producer warp, of which one lane issues every copy. S tile buffers cycle
-// through two mbarriers each: `full` (the tile's loads have landed; the
+// warps) and one producer warp, of which one lane issues every copy. S tile
+// buffers cycle through two mbarriers each: `full` (the tile's loads have landed; the
 // producer arrives with the byte count) and `empty` (all NT transform
 // threads have written the tile back). The producer stores a tile once it is
 // empty, waits until that store has read the buffer, and loads the tile S

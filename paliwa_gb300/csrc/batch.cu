@@ -319,11 +319,15 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
   int const log2G = lj.log2_n - log2r;
   if (encode == nullptr || lj.periodic != 1 || lj.base % 16 != 0)
     return false;
-  if (lj.log2_inner == 0 && lj.log2_kstride == 0) {
-    // The last axis (contiguous layout): the grid as rows of 32 floats (128
-    // bytes), boxes of the unit's 16 r rows, 128-byte swizzle; units of
-    // 512 r floats (whole pencils).
-    if (r < 4 || log2G < 0 || log2G > 5) return false;
+  bool const last = lj.log2_inner == 0 && lj.log2_kstride == 0;
+  bool const pairs = lj.log2_inner == 1 && lj.log2_kstride == 1 &&
+                     lj.log2_astride == lj.log2_n + 1;
+  if (last || pairs) {
+    // The last axis (contiguous layout), or a strided axis of inner extent
+    // 2 whose pencil pairs lie one after another (pairs layout): the
+    // stage's points as rows of 32 floats (128 bytes), boxes of the unit's
+    // 16 r rows, 128-byte swizzle; units of 512 r floats (whole pencils).
+    if (r < 4 || log2G < 0 || log2G > (pairs ? 2 : 5)) return false;
     long long const points = lj.columns << lj.log2_n;
     int const log2unit = 9 + log2r;
     int const log2u = r >= 8 ? 0 : 3 - log2r;  // units per tile
@@ -333,7 +337,7 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
     std::memset(&job, 0, sizeof(job));
     job.log2_n = lj.log2_n;
     job.nlevels = lj.nlevels;
-    job.chunked = 2;
+    job.chunked = pairs ? 3 : 2;
     job.nxb = 1;
     job.log2_bx = log2unit - lj.log2_n;  // box bytes = the unit
     job.log2_sx = 0;
@@ -501,8 +505,9 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
                   st.job.log2_inner == 0 && st.job.log2_kstride == 0;
               code = kTWide + r +
                      (last ? kTWideContig
-                           : log2G > 5 ? kTWideLong
-                                       : log2G >= 3 ? kTWideChunked : 0);
+                      : st.job.log2_inner == 1 ? kTWidePairs
+                      : log2G > 5 ? kTWideLong
+                      : log2G >= 3 ? kTWideChunked : 0);
             }
             by_r[code].push_back(&st);
           }

@@ -215,9 +215,15 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
                              wide_chunk(v.log2_n)))) <= 2) ||
        (R == 16 && log2G >= 3 && log2G <= 7)))
     k.mask |= 1 << kChooseTmaWide;
-  // ... and the last axis' wide stages of chunks of 4 to 16 points.
+  // ... and the last axis' wide stages of chunks of 4 to 16 points, and the
+  // wide stages of strided axes of inner extent 2 whose pencil pairs lie
+  // one after another.
   if (last && v.wide_last && k.has(kChooseWide) && R >= 4 &&
       v.base % 16 == 0)
+    k.mask |= 1 << kChooseTmaWide;
+  if (!last && v.wide_last && k.has(kChooseWide) && v.log2_inner == 1 &&
+      v.log2_kstride == 1 && v.log2_astride == v.log2_n + 1 &&
+      wide_chunk(v.log2_n) >= 4 && v.base % 16 == 0)
     k.mask |= 1 << kChooseTmaWide;
   // Default: the wide kernel for strided pencils (and FP32c last-axis
   // pencils: measured on 2^26-point grids, 3.0-4.5 TB/s against 2.8-4.1 on
@@ -247,10 +253,13 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   // staged kernel per launch (0.92 ms each) and the step 21.59 against
   // 22.02 ms with it; on the last axis 4.86 against 3.60 TB/s at 16 points,
   // 4.97 against 4.42 at 8 and 4.96 against 4.79 at 4 (the step 20.37
-  // against 21.20 ms). On strided 4-point chunks the wide kernel is faster,
-  // 5.26 against 4.39-4.55 TB/s.)
+  // against 21.20 ms); on strided axes of inner extent 2, 3.3-3.5 against
+  // 1.4-2.0 TB/s (20.15 against 20.30 ms). On strided 4-point chunks of
+  // wider inner extents the wide kernel is faster, 5.26 against 4.39-4.55
+  // TB/s.)
   if (k.has(kChooseTmaWide) &&
-      (last || wide_chunk(v.log2_n) >= 8 || !k.has(kChooseWide)))
+      (last || v.log2_inner == 1 || wide_chunk(v.log2_n) >= 8 ||
+       !k.has(kChooseWide)))
     k.dflt = kChooseTmaWide;
   return k;
 }

@@ -55,11 +55,12 @@ namespace pgb {
 constexpr int kTWideThreads = 256;               // transform threads
 constexpr int kTWideBlock = kTWideThreads + 32;  // + the producer warp
 // Added to the chunk size of a launch whose pencils have 8 to 32 chunks
-// (chunked form), more than 32 chunks (long form), or lie along the last
-// axis (contiguous form).
+// (chunked form), more than 32 chunks (long form), lie along the last axis
+// (contiguous form) or along a strided axis of inner extent 2 (pairs form).
 constexpr int kTWideChunked = 32;
 constexpr int kTWideLong = 64;
 constexpr int kTWideContig = 96;
+constexpr int kTWidePairs = 128;
 
 struct TWideJob {
   long long tile_begin;  // first tile of this job in the launch
@@ -71,7 +72,8 @@ struct TWideJob {
   int log2_sx;           // box: 2^log2_sx outer indices
   int nxb;               // boxes per tile
   int chunked;           // 1: the chunk-interleaved layout (G >= 8),
-                         // 2: the contiguous layout (the last axis)
+                         // 2: the contiguous layout (the last axis),
+                         // 3: the pairs layout (strided, inner extent 2)
   int log2_rs;           // floats between a thread's rows in shared memory
 };
 
@@ -179,12 +181,18 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
 // pencils' rows, fall on different banks (at most two lanes per bank
 // group). All forms exchange by shuffles and have no barrier after the
 // start. (One kernel for several forms kept more registers live and
-// spilled.) Longer pencils: twide_long_kernel below.
+// spilled.) 4, pencils of up to 4 chunks along a strided axis whose inner
+// extent is 2 columns (kstride 2, outer stride 2 n): a pencil pair's rows
+// are consecutive 8-byte pairs, so a unit is again 2 NT R consecutive
+// floats moved as swizzled 128-byte rows, and a thread's chunk is R / 2
+// consecutive 16-byte pieces of two rows each. Longer pencils:
+// twide_long_kernel below.
 template <class A, int R, class Sched, int FORM>
 __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     twide_kernel(__grid_constant__ const TWideParams p) {
   constexpr bool CHUNKED = FORM == 1;
-  constexpr bool CONTIG = FORM == 3;
+  constexpr bool PAIRS = FORM == 4;
+  constexpr bool CONTIG = FORM == 3 || PAIRS;
   using V = typename A::V;
   using W = typename A::Store;
   static_assert(sizeof(W) == 8, "rows of two float columns");
@@ -363,8 +371,8 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     // Jobs as the planner makes them for the launch's form (pencils of
     // more than 32 chunks would take exchange paths that need a barrier).
     bool const valid =
-        CONTIG ? R >= 4 && job.chunked == 2 &&
-                     static_cast<unsigned>(log2G) <= 5u
+        CONTIG ? R >= 4 && job.chunked == (PAIRS ? 3 : 2) &&
+                     static_cast<unsigned>(log2G) <= (PAIRS ? 2u : 5u)
                : (CHUNKED ? R == 16 && job.chunked == 1 && log2G >= 3 &&
                                 log2G <= 5
                           : !job.chunked &&
@@ -377,6 +385,36 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
         // whose chunk starts at float (2 g + e) n + c R of the unit.
         int const c = lane & ((1 << log2G) - 1);
         int const g = t >> log2G;
+        if constexpr (PAIRS) {
+          // Piece i of the chunk: rows 2 i and 2 i + 1 of both columns, at
+          // float 2 g n + 2 c R + 4 i of the unit.
+          auto piece = [&](int i) {
+            int const o =
+                (g << (job.log2_n + 1)) + (c << (LOG2R + 1)) + 4 * i;
+            int const row = o >> 5;
+            return (row << 7) + ((((o & 31) >> 2) ^ (row & 7)) << 4);
+          };
+          for (int u = 0; u < U; ++u) {
+            unsigned char *const ub = tiles + b * TILE + u * UNIT;
+            V v[R];
+#pragma unroll
+            for (int i = 0; i < R / 2; ++i) {
+              uint4 const f = *reinterpret_cast<uint4 const *>(ub + piece(i));
+              v[2 * i] = A::load(W{f.x, f.y});
+              v[2 * i + 1] = A::load(W{f.z, f.w});
+            }
+            RoundCtx<A, NT, true> ctx(t, c, 1 << log2G, log2G, lane, 1,
+                                      nullptr, nullptr);
+            Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
+#pragma unroll
+            for (int i = 0; i < R / 2; ++i) {
+              W const r0 = A::store(v[2 * i]);
+              W const r1 = A::store(v[2 * i + 1]);
+              *reinterpret_cast<uint4 *>(ub + piece(i)) =
+                  uint4{r0.x, r0.y, r1.x, r1.y};
+            }
+          }
+        } else {
         // The byte offset of piece i of column e: rows of 128 bytes, pieces
         // of 16 bytes swizzled within their row.
         auto piece = [&](int e, int i) {
@@ -410,6 +448,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
             *reinterpret_cast<uint4 *>(ub + piece(1, i)) =
                 uint4{r0.y, r1.y, r2.y, r3.y};
           }
+        }
         }
       } else if (lane == 0) {
         atomicExch(p.error, 1u);

@@ -54,6 +54,9 @@ void by_r(int R, TWideParams const &p, cudaStream_t s) {
   case kTWideContig + 4: return launch_twide_r<4, Sched, 3>(p, s);
   case kTWideContig + 8: return launch_twide_r<8, Sched, 3>(p, s);
   case kTWideContig + 16: return launch_twide_r<16, Sched, 3>(p, s);
+  case kTWidePairs + 4: return launch_twide_r<4, Sched, 4>(p, s);
+  case kTWidePairs + 8: return launch_twide_r<8, Sched, 4>(p, s);
+  case kTWidePairs + 16: return launch_twide_r<16, Sched, 4>(p, s);
   case kTWideLong + 16: return launch_twide_r<16, Sched, 2>(p, s);
   }
   throw StatusError(2, "twide launch with an unsupported chunk size");
@@ -62,8 +65,9 @@ void by_r(int R, TWideParams const &p, cudaStream_t s) {
 } // namespace
 
 // sched = 2 * wavelet + (forward ? 1 : 0); R = rows per chunk, plus
-// kTWideChunked for pencils of 8 to 32 chunks, kTWideLong for more, and
-// kTWideContig for the last axis.
+// kTWideChunked for pencils of 8 to 32 chunks, kTWideLong for more,
+// kTWideContig for the last axis and kTWidePairs for strided axes of inner
+// extent 2.
 void launch_twide_f32c(int sched, int R, TWideParams const &p,
                        cudaStream_t s) {
   switch (sched) {

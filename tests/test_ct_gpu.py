@@ -500,12 +500,12 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
               (1, 4, 9), (6, 2, 1), (2, 2, 2), (5, 5, 5), (4, 1, 10),
               (3, 2, 8), (2, 3, 6), (7, 4, 3), (8, 5, 1), (2, 8, 4),
               (7, 2, 2), (13, 2, 1), (9, 3, 2), (2, 9, 4), (10, 2, 3),
-              (3, 11, 2), (11, 1, 4)]
+              (3, 11, 2), (11, 1, 4), (2, 6, 1), (3, 4, 1)]
     lmin, lmax = (1, 1, 1), (14, 14, 14)
     rng = np.random.default_rng(78)
     host = [rng.uniform(-1, 1, 1 << sum(l)).astype(np.float32)
             for l in levels]
-    seen, seen_last = set(), set()
+    seen, seen_last, seen_pairs = set(), set(), set()
     for wavelet in ("hat", "biorthogonal", "fullweighting"):
         out = []
         for kernel in ("twide", "other"):
@@ -531,6 +531,10 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
                     seen_last.update(d["log2_n"] for c, d, _, _ in
                                      b.tuning(forward)
                                      if c in cls and d["last"])
+                    seen_pairs.update(d["log2_n"] for c, d, _, _ in
+                                      b.tuning(forward)
+                                      if c in cls and not d["last"] and
+                                      d["log2_inner_bytes"] == 3)
             s = torch.cuda.Stream()
             kernels = b.profile(True, stream=s)[2]
             assert any(k > pct.TWIDE_KERNEL for k in kernels) == \
@@ -560,3 +564,5 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
     # do), strided and along the last axis
     assert {2, 3, 4, 5, 6, 7, 8, 9, 10, 11} <= seen, seen
     assert {2, 3, 4, 5, 6} <= seen_last, seen_last
+    # strided axes of inner extent 2 (8 bytes per row)
+    assert {2, 4, 5, 6} <= seen_pairs, seen_pairs

@@ -375,17 +375,26 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
     job.nxb = 1;
     job.log2_bx = std::min(lj.log2_inner, log2ct);  // Bx >= 4: log2ct <= 6
     job.log2_sx = log2ct - job.log2_bx;
-    job.log2_rs = log2G + 2;
-    cuuint64_t dims[5] = {4, static_cast<cuuint64_t>(1) << log2G,
+    // Groups of 8 columns (32-byte box rows) where the tile and the inner
+    // extent hold them, else 4 (16 bytes, the least a box row may be):
+    // wider rows halve the rows the tensor memory accelerator moves (the
+    // chunked form: 3.91 against 3.5 TB/s on the 4D batch). Not for more
+    // than 32 chunks, whose warps would read 8-way conflicting banks (the
+    // long form measured slower with them).
+    int const xlo = log2ct >= 3 && lj.log2_inner >= 3 && log2G <= 5 ? 3 : 2;
+    job.log2_xlo = xlo;
+    job.log2_rs = log2G + xlo;
+    cuuint64_t dims[5] = {1u << xlo, static_cast<cuuint64_t>(1) << log2G,
                           static_cast<cuuint64_t>(r),
-                          static_cast<cuuint64_t>(1) << (lj.log2_inner - 2),
+                          static_cast<cuuint64_t>(1) << (lj.log2_inner - xlo),
                           static_cast<cuuint64_t>(outer)};
     cuuint64_t strides[4] = {
         static_cast<cuuint64_t>(4 * r) << lj.log2_kstride,
-        static_cast<cuuint64_t>(4) << lj.log2_kstride, 16,
+        static_cast<cuuint64_t>(4) << lj.log2_kstride,
+        static_cast<cuuint64_t>(4) << xlo,
         static_cast<cuuint64_t>(4) << lj.log2_astride};
-    cuuint32_t box[5] = {4, 1u << log2G, static_cast<cuuint32_t>(r),
-                         1u << (job.log2_bx - 2), 1u << job.log2_sx};
+    cuuint32_t box[5] = {1u << xlo, 1u << log2G, static_cast<cuuint32_t>(r),
+                         1u << (job.log2_bx - xlo), 1u << job.log2_sx};
     cuuint32_t elem[5] = {1, 1, 1, 1, 1};
     CUresult const res = encode(
         &map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5,

@@ -75,6 +75,7 @@ struct TWideJob {
                          // 2: the contiguous layout (the last axis),
                          // 3: the pairs layout (strided, inner extent 2)
   int log2_rs;           // floats between a thread's rows in shared memory
+  int log2_xlo;          // chunk-interleaved layout: columns per group
 };
 
 struct TWideParams {
@@ -102,6 +103,16 @@ __device__ __forceinline__ void tma_store_3d(void const *map, int x, int y,
       "%3}], [%4];\n" ::"l"(reinterpret_cast<unsigned long long>(map)),
       "r"(x), "r"(y), "r"(z), "r"(smem_u32(src))
       : "memory");
+}
+// Chunk-interleaved layout, [column group][row of chunk][chunk][X columns]
+// (X = 2^log2_xlo, 4 or 8): the float index of row 0 of chunk c of column
+// pair g (rows follow X G floats apart).
+template <int LOG2R>
+__device__ __forceinline__ int chunk_index(TWideJob const &job, int g, int c,
+                                           int log2G) {
+  int const x = job.log2_xlo;
+  return (((((g >> (x - 1)) << LOG2R) << log2G) + c) << x) +
+         2 * (g & ((1 << (x - 1)) - 1));
 }
 // Orders the host's writes of a tensor map in global memory before its use
 // by the tensor memory accelerator.
@@ -282,7 +293,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
         continue;
       }
       if (job.chunked) {  // one box: the unit (nxb = 1)
-        tma_load_5d(dst, map, x0 >> 2, z0, &full[b]);
+        tma_load_5d(dst, map, x0 >> job.log2_xlo, z0, &full[b]);
         continue;
       }
       for (int xb = 0; xb < job.nxb; ++xb) {
@@ -308,7 +319,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
         continue;
       }
       if (job.chunked) {
-        tma_store_5d(map, x0 >> 2, z0, src);
+        tma_store_5d(map, x0 >> job.log2_xlo, z0, src);
         continue;
       }
       for (int xb = 0; xb < job.nxb; ++xb) {
@@ -377,7 +388,9 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
                                 log2G <= 5
                           : !job.chunked &&
                                 static_cast<unsigned>(log2G) <= 2u) &&
-                     job.log2_rs == (CHUNKED ? log2G + 2 : job.log2_bx);
+                     job.log2_rs ==
+                         (CHUNKED ? log2G + job.log2_xlo : job.log2_bx) &&
+                     (!CHUNKED || (job.log2_xlo >= 2 && job.log2_xlo <= 3));
     if constexpr (CONTIG) {
       if (valid) {
         // Thread = (chunk c, column pair g): the G chunks of a pencil pair
@@ -466,7 +479,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
       int idx0;
       if constexpr (CHUNKED) {
         // [column quad][row of chunk][chunk][4 columns]
-        idx0 = (((((g >> 1) << LOG2R) << log2G) + c) << 2) + 2 * (g & 1);
+        idx0 = chunk_index<LOG2R>(job, g, c, log2G);
       } else {
         int const col = 2 * g;
         int const log2bs = job.log2_bx + job.log2_sx;
@@ -556,7 +569,8 @@ __global__ void __launch_bounds__(kTWideThreads, 2)
     int const log2ct = LOG2NT + 1 - (job.log2_n - LOG2R);
     long long const col0 = (tile - job.tile_begin) << log2ct;
     z0 = static_cast<int>(col0 >> job.log2_inner);
-    q0 = static_cast<int>((col0 & ((1LL << job.log2_inner) - 1)) >> 2);
+    q0 = static_cast<int>((col0 & ((1LL << job.log2_inner) - 1)) >>
+                          job.log2_xlo);
   };
   auto issue_load = [&](long long k) {
     int const b = static_cast<int>(k % S);
@@ -606,14 +620,15 @@ __global__ void __launch_bounds__(kTWideThreads, 2)
     int const log2G = job.log2_n - LOG2R;
     // Jobs as the planner makes them (uniform over the tile, so every
     // thread takes the same barriers).
-    if (job.chunked && log2G >= 6 && log2G <= 7 && job.log2_rs == log2G + 2) {
+    if (job.chunked && log2G >= 6 && log2G <= 7 && job.log2_xlo >= 2 &&
+        job.log2_xlo <= 3 && job.log2_rs == log2G + job.log2_xlo) {
       int const G = 1 << log2G;
       // Thread = (chunk c, column pair g): chunks in consecutive threads.
       int const c = t & (G - 1);
       int const g = t >> log2G;
       // [column quad][row of chunk][chunk][4 columns]
       int const idx0 =
-          (((((g >> 1) << LOG2R) << log2G) + c) << 2) + 2 * (g & 1);
+          chunk_index<LOG2R>(job, g, c, log2G);
       float *const tf = reinterpret_cast<float *>(tiles + b * TILE);
       V v[R];
 #pragma unroll

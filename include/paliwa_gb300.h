@@ -258,7 +258,7 @@ int paliwa_gb_batch_use_slabs(paliwa_gb_batch *batch, int enable);
 /* enable != 0 (default): FP32-compensated stages of strided pencils of up
  * to 2048 points (up to 128 chunks; inner extent of 4 or more columns, or
  * of 2 with the pencil pairs one after another) and of the last axis'
- * pencils of up to 512 points, in 16-byte aligned grids,
+ * pencils of up to 4096 points, in 16-byte aligned grids,
  * may run on the TMA wide kernel: the wide kernel's register transform,
  * with each tile moved between HBM and shared memory by bulk tensor copies
  * over a tensor map of the grid's axis (bounded waits, reported by
@@ -294,8 +294,8 @@ int paliwa_gb_batch_info(const paliwa_gb_batch *batch, int64_t *points,
  * the slab kernel (every level of a grid's
  * trailing axes in one pass; its bytes count one read and one write of each
  * point), 2048 + R the TMA wide kernel (+ 32: pencils of 8 to 32 chunks,
- * + 64: more, + 96: the last axis, + 128: inner extent 2); `kernels` may
- * be null. Call with
+ * + 64: more, + 96: the last axis, + 160: its pencils of more than 32
+ * chunks, + 128: inner extent 2); `kernels` may be null. Call with
  * capacity 0 to get *nlaunches first. */
 int paliwa_gb_batch_profile(paliwa_gb_batch *batch, int forward, void *stream,
                             int capacity, int *nlaunches, float *ms,

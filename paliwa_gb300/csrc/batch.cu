@@ -296,8 +296,9 @@ int twide_chunk(Stage const &st) {
     return R - kWide;
   if (R == kWideContig + 4 || R == kWideContig + 8 || R == kWideContig + 16)
     return R - kWideContig;
+  bool const last = st.job.log2_inner == 0 && st.job.log2_kstride == 0;
   if ((R == kTile + 16 || R == kTileLong + 16 || R == 16 || R == 32) &&
-      st.job.log2_n >= 7 && st.job.log2_n <= 11)
+      st.job.log2_n >= 7 && st.job.log2_n <= (last ? 12 : 11))
     return 16;
   return 0;
 }
@@ -327,7 +328,8 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
     // 2 whose pencil pairs lie one after another (pairs layout): the
     // stage's points as rows of 32 floats (128 bytes), boxes of the unit's
     // 16 r rows, 128-byte swizzle; units of 512 r floats (whole pencils).
-    if (r < 4 || log2G < 0 || log2G > (pairs ? 2 : 5)) return false;
+    if (r < 4 || log2G < 0 || log2G > (pairs ? 2 : 5 + 3 * (r == 16)))
+      return false;
     long long const points = lj.columns << lj.log2_n;
     int const log2unit = 9 + log2r;
     int const log2u = r >= 8 ? 0 : 3 - log2r;  // units per tile
@@ -513,7 +515,7 @@ void plan_direction(paliwa_gb_batch &b, Direction &dr, bool forward,
               bool const last =
                   st.job.log2_inner == 0 && st.job.log2_kstride == 0;
               code = kTWide + r +
-                     (last ? kTWideContig
+                     (last ? (log2G > 5 ? kTWideLongContig : kTWideContig)
                       : st.job.log2_inner == 1 ? kTWidePairs
                       : log2G > 5 ? kTWideLong
                       : log2G >= 3 ? kTWideChunked : 0);

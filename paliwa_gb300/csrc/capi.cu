@@ -215,11 +215,13 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
                              wide_chunk(v.log2_n)))) <= 2) ||
        (R == 16 && log2G >= 3 && log2G <= 7)))
     k.mask |= 1 << kChooseTmaWide;
-  // ... and the last axis' wide stages of chunks of 4 to 16 points, and the
+  // ... and the last axis' wide stages of chunks of 4 to 16 points and its
+  // pencils of 64 to 256 chunks of 16 points (1024 to 4096 points), and the
   // wide stages of strided axes of inner extent 2 whose pencil pairs lie
   // one after another.
-  if (last && v.wide_last && k.has(kChooseWide) && R >= 4 &&
-      v.base % 16 == 0)
+  if (last && v.wide_last && v.base % 16 == 0 &&
+      ((k.has(kChooseWide) && R >= 4) ||
+       (R == 16 && log2G >= 6 && log2G <= 8)))
     k.mask |= 1 << kChooseTmaWide;
   if (!last && v.wide_last && k.has(kChooseWide) && v.log2_inner == 1 &&
       v.log2_kstride == 1 && v.log2_astride == v.log2_n + 1 &&
@@ -253,8 +255,10 @@ KernelSet periodic_kernels(AxisView const &v, bool canon) {
   // staged kernel per launch (0.92 ms each) and the step 21.59 against
   // 22.02 ms with it; on the last axis 4.86 against 3.60 TB/s at 16 points,
   // 4.97 against 4.42 at 8 and 4.96 against 4.79 at 4 (the step 20.37
-  // against 21.20 ms); on strided axes of inner extent 2, 3.3-3.5 against
-  // 1.4-2.0 TB/s (20.15 against 20.30 ms). On strided 4-point chunks of
+  // against 21.20 ms), and on its pencils of 1024-4096 points 0.39 against
+  // 0.41 ms on the staged kernel (19.71 against 19.81 ms); on strided axes
+  // of inner extent 2, 3.3-3.5 against 1.4-2.0 TB/s (20.15 against 20.30
+  // ms). On strided 4-point chunks of
   // wider inner extents the wide kernel is faster, 5.26 against 4.39-4.55
   // TB/s.)
   if (k.has(kChooseTmaWide) &&

@@ -56,11 +56,13 @@ constexpr int kTWideThreads = 256;               // transform threads
 constexpr int kTWideBlock = kTWideThreads + 32;  // + the producer warp
 // Added to the chunk size of a launch whose pencils have 8 to 32 chunks
 // (chunked form), more than 32 chunks (long form), lie along the last axis
-// (contiguous form) or along a strided axis of inner extent 2 (pairs form).
+// (contiguous form; more than 32 chunks: long contiguous form) or along a
+// strided axis of inner extent 2 (pairs form).
 constexpr int kTWideChunked = 32;
 constexpr int kTWideLong = 64;
 constexpr int kTWideContig = 96;
 constexpr int kTWidePairs = 128;
+constexpr int kTWideLongContig = 160;
 
 struct TWideJob {
   long long tile_begin;  // first tile of this job in the launch
@@ -518,7 +520,10 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
 
 
 // Long form: periodic pencils of 64 or 128 chunks of 16 points (1024 and
-// 2048 points) in the chunk-interleaved layout. Their chunks are
+// 2048 points) in the chunk-interleaved layout, or (CONTIG) the last axis'
+// pencils of 64 to 256 chunks (1024 to 4096 points) in the contiguous
+// layout (a tile is whole pencils: 2 NT R consecutive floats, as swizzled
+// 128-byte rows, see FORM 3 of twide_kernel). Their chunks are
 // consecutive threads and exchange through shared memory with a CTA barrier
 // per step, so every thread meets at barriers anyway: there is no producer
 // warp. Thread 0 issues the copies right after each tile's vote barrier
@@ -527,7 +532,7 @@ __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
 // tile's store has read it. 256 threads per CTA leave 128 registers per
 // thread for two CTAs per SM (a producer warp would leave 96, and the form
 // spilled there).
-template <class A, class Sched>
+template <class A, class Sched, bool CONTIG>
 __global__ void __launch_bounds__(kTWideThreads, 2)
     twide_long_kernel(__grid_constant__ const TWideParams p) {
   using V = typename A::V;
@@ -543,7 +548,7 @@ __global__ void __launch_bounds__(kTWideThreads, 2)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned const base_addr = smem_u32(smem_raw);
   unsigned char *const tiles =
-      smem_raw + ((128 - (base_addr & 127)) & 127);  // 128-byte aligned
+      smem_raw + ((1024 - (base_addr & 1023)) & 1023);  // swizzle atoms
   V *const heads = reinterpret_cast<V *>(tiles + S * TILE);
   V *const xch = heads + NT;
   __shared__ uint64_t full[S];
@@ -562,8 +567,8 @@ __global__ void __launch_bounds__(kTWideThreads, 2)
   }
   __syncthreads();
 
-  // Thread 0's copies (one 5D box per tile); it keeps the last map it
-  // fenced.
+  // Thread 0's copies (one box per tile: 5D, or 2D of 16 R rows of 128
+  // bytes); it keeps the last map it fenced.
   int fenced = -1;
   auto origin = [](TWideJob const &job, long long tile, int &q0, int &z0) {
     int const log2ct = LOG2NT + 1 - (job.log2_n - LOG2R);
@@ -583,17 +588,29 @@ __global__ void __launch_bounds__(kTWideThreads, 2)
       fenced = job.map;
     }
     mbar_expect_tx(&full[b], static_cast<unsigned>(TILE));
-    int q0, z0;
-    origin(job, tile, q0, z0);
-    tma_load_5d(tiles + b * TILE, map, q0, z0, &full[b]);
+    if constexpr (CONTIG) {
+      tma_load_2d(tiles + b * TILE, reinterpret_cast<CUtensorMap const *>(map),
+                  0, static_cast<int>((tile - job.tile_begin) << (LOG2R + 4)),
+                  &full[b]);
+    } else {
+      int q0, z0;
+      origin(job, tile, q0, z0);
+      tma_load_5d(tiles + b * TILE, map, q0, z0, &full[b]);
+    }
   };
   auto issue_store = [&](long long k) {
     int const b = static_cast<int>(k % S);
     long long const tile = first + k * step;
     TWideJob const &job = sjob[b];
-    int q0, z0;
-    origin(job, tile, q0, z0);
-    tma_store_5d(p.maps + job.map, q0, z0, tiles + b * TILE);
+    if constexpr (CONTIG) {
+      tma_store_2d(reinterpret_cast<CUtensorMap const *>(p.maps + job.map), 0,
+                   static_cast<int>((tile - job.tile_begin) << (LOG2R + 4)),
+                   tiles + b * TILE);
+    } else {
+      int q0, z0;
+      origin(job, tile, q0, z0);
+      tma_store_5d(p.maps + job.map, q0, z0, tiles + b * TILE);
+    }
     bulk_commit();
   };
 
@@ -620,15 +637,55 @@ __global__ void __launch_bounds__(kTWideThreads, 2)
     int const log2G = job.log2_n - LOG2R;
     // Jobs as the planner makes them (uniform over the tile, so every
     // thread takes the same barriers).
-    if (job.chunked && log2G >= 6 && log2G <= 7 && job.log2_xlo >= 2 &&
-        job.log2_xlo <= 3 && job.log2_rs == log2G + job.log2_xlo) {
+    if constexpr (CONTIG) {
+      if (job.chunked == 2 && log2G >= 6 && log2G <= 8) {
+        int const G = 1 << log2G;
+        // Thread = (chunk c, pencil pair g): chunks in consecutive threads;
+        // column e of the pair is pencil 2 g + e, whose chunk starts at
+        // float (2 g + e) n + c R of the tile.
+        int const c = t & (G - 1);
+        int const g = t >> log2G;
+        auto piece = [&](int e, int i) {
+          int const o = ((2 * g + e) << job.log2_n) + (c << LOG2R);
+          int const row = o >> 5;
+          return (row << 7) + (((((o & 31) >> 2) + i) ^ (row & 7)) << 4);
+        };
+        unsigned char *const ub = tiles + b * TILE;
+        V v[R];
+#pragma unroll
+        for (int i = 0; i < R / 4; ++i) {
+          uint4 const f0 = *reinterpret_cast<uint4 const *>(ub + piece(0, i));
+          uint4 const f1 = *reinterpret_cast<uint4 const *>(ub + piece(1, i));
+          v[4 * i] = A::load(W{f0.x, f1.x});
+          v[4 * i + 1] = A::load(W{f0.y, f1.y});
+          v[4 * i + 2] = A::load(W{f0.z, f1.z});
+          v[4 * i + 3] = A::load(W{f0.w, f1.w});
+        }
+        RoundCtx<A, NT, false, 256> ctx(t, c, G, log2G, lane, 1, heads, xch);
+        Sched::template run_levels<A, R, NT>(v, ctx, job.nlevels);
+#pragma unroll
+        for (int i = 0; i < R / 4; ++i) {
+          W const r0 = A::store(v[4 * i]);
+          W const r1 = A::store(v[4 * i + 1]);
+          W const r2 = A::store(v[4 * i + 2]);
+          W const r3 = A::store(v[4 * i + 3]);
+          *reinterpret_cast<uint4 *>(ub + piece(0, i)) =
+              uint4{r0.x, r1.x, r2.x, r3.x};
+          *reinterpret_cast<uint4 *>(ub + piece(1, i)) =
+              uint4{r0.y, r1.y, r2.y, r3.y};
+        }
+      } else if (t == 0) {
+        atomicExch(p.error, 1u);
+      }
+    } else if (job.chunked == 1 && log2G >= 6 && log2G <= 7 &&
+               job.log2_xlo >= 2 && job.log2_xlo <= 3 &&
+               job.log2_rs == log2G + job.log2_xlo) {
       int const G = 1 << log2G;
       // Thread = (chunk c, column pair g): chunks in consecutive threads.
       int const c = t & (G - 1);
       int const g = t >> log2G;
-      // [column quad][row of chunk][chunk][4 columns]
-      int const idx0 =
-          chunk_index<LOG2R>(job, g, c, log2G);
+      // [column group][row of chunk][chunk][X columns]
+      int const idx0 = chunk_index<LOG2R>(job, g, c, log2G);
       float *const tf = reinterpret_cast<float *>(tiles + b * TILE);
       V v[R];
 #pragma unroll

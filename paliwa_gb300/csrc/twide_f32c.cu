@@ -10,11 +10,11 @@ namespace {
 template <int R, class Sched, int FORM>
 void launch_twide_r(TWideParams const &p, cudaStream_t s) {
   static thread_local Occupancy occ;
-  constexpr bool kLong = FORM == 2;
+  constexpr bool kLong = FORM == 2 || FORM == 5;
   constexpr int kBlock = kLong ? kTWideThreads : kTWideBlock;
   auto kernel = [] {
     if constexpr (kLong)
-      return twide_long_kernel<RowF32C, Sched>;
+      return twide_long_kernel<RowF32C, Sched, FORM == 5>;
     else
       return twide_kernel<RowF32C, R, Sched, FORM>;
   }();
@@ -58,6 +58,7 @@ void by_r(int R, TWideParams const &p, cudaStream_t s) {
   case kTWidePairs + 8: return launch_twide_r<8, Sched, 4>(p, s);
   case kTWidePairs + 16: return launch_twide_r<16, Sched, 4>(p, s);
   case kTWideLong + 16: return launch_twide_r<16, Sched, 2>(p, s);
+  case kTWideLongContig + 16: return launch_twide_r<16, Sched, 5>(p, s);
   }
   throw StatusError(2, "twide launch with an unsupported chunk size");
 }
@@ -66,8 +67,8 @@ void by_r(int R, TWideParams const &p, cudaStream_t s) {
 
 // sched = 2 * wavelet + (forward ? 1 : 0); R = rows per chunk, plus
 // kTWideChunked for pencils of 8 to 32 chunks, kTWideLong for more,
-// kTWideContig for the last axis and kTWidePairs for strided axes of inner
-// extent 2.
+// kTWideContig for the last axis (kTWideLongContig for its pencils of more
+// than 32 chunks) and kTWidePairs for strided axes of inner extent 2.
 void launch_twide_f32c(int sched, int R, TWideParams const &p,
                        cudaStream_t s) {
   switch (sched) {

@@ -69,18 +69,23 @@ def packed_grids(levels, dtype, device="cuda", align=64):
 
 
 # Launch codes of the slab kernel and (plus the chunk size, plus 32 for
-# pencils of 8 to 32 chunks, 64 for more, 96 for the last axis and 128 for
-# strided axes of inner extent 2) of the TMA wide kernel in Batch.profile.
+# pencils of 8 to 32 chunks, 64 for more, 96 for the last axis, 160 for its
+# pencils of more than 32 chunks and 128 for strided axes of inner extent 2)
+# of the TMA wide kernel in Batch.profile.
 SLAB_KERNEL = 1024
 TWIDE_KERNEL = 2048
 TWIDE_CHUNKED = 32
 TWIDE_LONG = 64
 TWIDE_CONTIG = 96
 TWIDE_PAIRS = 128
+TWIDE_LONG_CONTIG = 160
 
 
 def kernel_name(code):
     """Name of the lifting kernel behind a launch code of Batch.profile."""
+    if code > TWIDE_KERNEL + TWIDE_LONG_CONTIG:
+        return ("twide_kernel long last axis "
+                f"R={code - TWIDE_KERNEL - TWIDE_LONG_CONTIG}")
     if code > TWIDE_KERNEL + TWIDE_PAIRS:
         return ("twide_kernel inner 2 "
                 f"R={code - TWIDE_KERNEL - TWIDE_PAIRS}")

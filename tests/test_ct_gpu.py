@@ -500,7 +500,8 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
               (1, 4, 9), (6, 2, 1), (2, 2, 2), (5, 5, 5), (4, 1, 10),
               (3, 2, 8), (2, 3, 6), (7, 4, 3), (8, 5, 1), (2, 8, 4),
               (7, 2, 2), (13, 2, 1), (9, 3, 2), (2, 9, 4), (10, 2, 3),
-              (3, 11, 2), (11, 1, 4), (2, 6, 1), (3, 4, 1)]
+              (3, 11, 2), (11, 1, 4), (2, 6, 1), (3, 4, 1), (2, 2, 11),
+              (2, 1, 12)]
     lmin, lmax = (1, 1, 1), (14, 14, 14)
     rng = np.random.default_rng(78)
     host = [rng.uniform(-1, 1, 1 << sum(l)).astype(np.float32)
@@ -563,6 +564,6 @@ def test_every_tma_wide_class_gives_the_wide_kernels_bits():
     # pencils of 4 to 2048 points (axes at level 1 = lmin have nothing to
     # do), strided and along the last axis
     assert {2, 3, 4, 5, 6, 7, 8, 9, 10, 11} <= seen, seen
-    assert {2, 3, 4, 5, 6} <= seen_last, seen_last
+    assert {2, 3, 4, 5, 6, 10, 11, 12} <= seen_last, seen_last
     # strided axes of inner extent 2 (8 bytes per row)
     assert {2, 4, 5, 6} <= seen_pairs, seen_pairs

@@ -37,3 +37,25 @@ def test_group_ranges_cover_in_order():
         assert len(r) <= max(1, min(groups, len(sizes)))
     r = group_ranges([1] * 64, 8)
     assert [b - a for a, b in r] == [8] * 8
+
+
+def test_launch_code_names():
+    """Batch.profile's launch codes (include/paliwa_gb300.h): staged, direct,
+    wide, tile, halo and slab kernels, and the TMA wide kernel's forms
+    (2048 + R, plus 32 / 64 / 96 / 128 / 160 for the chunked, long, last
+    axis, inner extent 2 and long last-axis forms)."""
+    from paliwa_gb300 import ct as pct
+    names = {
+        32: "lift_kernel staged R=32", -16: "lift_kernel direct R=16",
+        64 + 8: "wide_kernel R=8", 128 + 16: "wide_kernel last axis R=16",
+        192 + 16: "tile_kernel R=16", 256 + 16: "tile_kernel long R=16",
+        512: "halo_kernel", 1024: "slab_kernel",
+        2048 + 16: "twide_kernel R=16",
+        2048 + 32 + 16: "twide_kernel chunked R=16",
+        2048 + 64 + 16: "twide_kernel long R=16",
+        2048 + 96 + 4: "twide_kernel last axis R=4",
+        2048 + 128 + 8: "twide_kernel inner 2 R=8",
+        2048 + 160 + 16: "twide_kernel long last axis R=16",
+    }
+    for code, name in names.items():
+        assert pct.kernel_name(code) == name, (code, pct.kernel_name(code))

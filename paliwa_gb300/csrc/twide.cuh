@@ -1,26 +1,29 @@
 // TMA wide kernel: the wide kernel's register transform (rows of two
 // adjacent columns as double-float f32x2 pairs, chunks of one pencil in
 // lanes, shuffles) for strided pencils of up to 2048 points (G <= 128
-// chunks) and the last axis' pencils of up to 512 points, with the data
+// chunks) and the last axis' pencils of up to 4096 points, with the data
 // moved by the tensor memory accelerator instead of per-thread copies.
 //
 // A tile is one unit of the wide kernel (several for chunks of up to 8
 // points): NT threads x R rows x 2 columns = Ct = 2 NT / G consecutive
 // columns (column = (outer index, inner index)) of all n rows of their
-// pencils. Each grid and axis has a tensor map, in one of three layouts:
+// pencils. Each grid and axis has a tensor map, in one of four layouts:
 //  * dense (up to 4 chunks): a 3D map over the [outer][n][inner] view
 //    (strides of the axis: sub-lattices included); a tile is 1 or 2 boxes
 //    {Bx columns of one outer index, n rows, Sx outer indices} (Bx =
 //    min(inner, Ct, 256), Sx = Ct / inner when inner < Ct), in shared
 //    memory as [box][outer][row][column];
-//  * chunk-interleaved (8 to 128 chunks of 16 points): a 5D map {4 columns,
-//    G chunks, R rows of a chunk, column quads, outer index} and one box per
-//    tile, in shared memory as [column quad][row of chunk][chunk][4
-//    columns], so that the chunks a warp reads together lie in consecutive
-//    16-byte groups (with the dense layout they would read rows R apart, on
-//    the same banks; a pad after a box per chunk is not possible, since
-//    bulk tensor copies need 128-byte aligned shared-memory destinations);
-//  * contiguous (the last axis): see FORM 3 of twide_kernel.
+//  * chunk-interleaved (8 to 128 chunks of 16 points): a 5D map {X columns,
+//    G chunks, R rows of a chunk, column groups, outer index} (X = 4 or 8)
+//    and one box per tile, in shared memory as [column group][row of
+//    chunk][chunk][X columns], so that the chunks a warp reads together lie
+//    in consecutive X-column groups (with the dense layout they would read
+//    rows R apart, on the same banks; a pad after a box per chunk is not
+//    possible, since bulk tensor copies need 128-byte aligned shared-memory
+//    destinations);
+//  * contiguous (the last axis) and pairs (strided, inner extent 2): the
+//    stage's points as 128-byte rows of a 2D map with the 128-byte swizzle,
+//    see FORMs 3 and 4 of twide_kernel.
 // Completion is on an mbarrier with a bounded wait. After the transform the
 // threads write their rows back into the same place and one thread stores
 // the boxes with bulk tensor stores. Columns past the end of the grid are
@@ -31,14 +34,15 @@
 //
 // twide_kernel's CTA is warp-specialised: NT transform threads (eight
 // warps) and one producer warp, of which one lane issues every copy. S tile
-// buffers cycle through two mbarriers each: `full` (the tile's loads have landed; the
-// producer arrives with the byte count) and `empty` (all NT transform
-// threads have written the tile back). The producer stores a tile once it is
-// empty, waits until that store has read the buffer, and loads the tile S
-// later into it; the transform warps never meet at a CTA barrier and never
-// wait for a store (a version with one CTA barrier per tile and the copies
-// issued by thread 0 between tiles stalled on the barrier more than on
-// anything else).
+// buffers cycle through two mbarriers each: `full` (the tile's loads have
+// landed; the producer arrives with the byte count) and `empty` (all NT
+// transform threads have written the tile back). The producer stores a
+// tile once it is empty, waits until that store has read the buffer, and
+// loads the tile S later into it; the transform warps never meet at a CTA
+// barrier and never wait for a store (a version with one CTA barrier per
+// tile and the copies issued by thread 0 between tiles stalled on the
+// barrier more than on anything else). twide_long_kernel (pencils of more
+// than 32 chunks) has no producer warp; see there.
 //
 // The maps live in global memory, written by the host before the launch;
 // they cover only this GPU's grid memory (no multicast).
@@ -73,9 +77,10 @@ struct TWideJob {
   int log2_bx;           // box: 2^log2_bx columns of one outer index
   int log2_sx;           // box: 2^log2_sx outer indices
   int nxb;               // boxes per tile
-  int chunked;           // 1: the chunk-interleaved layout (G >= 8),
-                         // 2: the contiguous layout (the last axis),
-                         // 3: the pairs layout (strided, inner extent 2)
+  int chunked;           // 0: the dense layout, 1: the chunk-interleaved
+                         // layout (G >= 8), 2: the contiguous layout (the
+                         // last axis), 3: the pairs layout (strided,
+                         // inner extent 2)
   int log2_rs;           // floats between a thread's rows in shared memory
   int log2_xlo;          // chunk-interleaved layout: columns per group
 };

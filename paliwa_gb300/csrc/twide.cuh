@@ -189,22 +189,24 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
   return true;
 }
 
-// FORM (the same for every job of a launch): 0, pencils of up to 4 chunks in
-// the dense layout; 1, pencils of 8 to 32 chunks of 16 points in the
-// chunk-interleaved layout; 3, last-axis pencils of up to 32 chunks of 4, 8
-// or 16 points in the contiguous layout: a unit is 2 NT R consecutive
-// floats (whole pencils), moved as 128-byte rows of a 2D tensor map with
-// the 128-byte swizzle (16-byte piece q of row r stored at q ^ (r mod 8)),
-// so that the lanes of a warp, each reading 16-byte pieces of its own
-// pencils' rows, fall on different banks (at most two lanes per bank
-// group). All forms exchange by shuffles and have no barrier after the
-// start. (One kernel for several forms kept more registers live and
-// spilled.) 4, pencils of up to 4 chunks along a strided axis whose inner
-// extent is 2 columns (kstride 2, outer stride 2 n): a pencil pair's rows
-// are consecutive 8-byte pairs, so a unit is again 2 NT R consecutive
-// floats moved as swizzled 128-byte rows, and a thread's chunk is R / 2
-// consecutive 16-byte pieces of two rows each. Longer pencils:
-// twide_long_kernel below.
+// FORM (the same for every job of a launch):
+//  0, pencils of up to 4 chunks in the dense layout;
+//  1, pencils of 8 to 32 chunks of 16 points in the chunk-interleaved
+//     layout;
+//  3, last-axis pencils of up to 32 chunks of 4, 8 or 16 points in the
+//     contiguous layout: a unit is 2 NT R consecutive floats (whole
+//     pencils), moved as 128-byte rows of a 2D tensor map with the 128-byte
+//     swizzle (16-byte piece q of row r stored at q ^ (r mod 8)), so that
+//     the lanes of a warp, each reading 16-byte pieces of its own pencils'
+//     rows, fall on different banks (at most two lanes per bank group);
+//  4, pencils of up to 4 chunks along a strided axis whose inner extent is
+//     2 columns (kstride 2, outer stride 2 n): a pencil pair's rows are
+//     consecutive 8-byte pairs, so a unit is again 2 NT R consecutive floats
+//     moved as swizzled 128-byte rows, and a thread's chunk is R / 2
+//     consecutive 16-byte pieces of two rows each.
+// All forms exchange by shuffles and have no barrier after the start. (One
+// kernel for several forms kept more registers live and spilled.) Longer
+// pencils (form 2 and 5 of the launch codes): twide_long_kernel below.
 template <class A, int R, class Sched, int FORM>
 __global__ void __launch_bounds__(kTWideBlock, R >= 16 ? 2 : 3)
     twide_kernel(__grid_constant__ const TWideParams p) {

@@ -412,6 +412,22 @@ bool twide_job(Stage const &st, int r, TWideJob &job, CUtensorMap &map,
                            static_cast<cuuint64_t>(4) << lj.log2_astride};
   cuuint32_t box[3] = {1u << job.log2_bx, 1u << lj.log2_n,
                        1u << job.log2_sx};
+  // An outer index's n rows of `inner` columns are one contiguous block
+  // when the pencil stride is the inner extent (no sub-lattice). When a
+  // tile holds whole blocks (inner < Ct) and a block fits one box
+  // dimension, the map takes the block as its rows: box rows of n inner
+  // floats instead of inner (fewer, longer rows for the tensor memory
+  // accelerator), the same bytes in the same shared-memory order, the same
+  // box coordinates (x = y = 0).
+  if (lj.log2_kstride == lj.log2_inner && lj.log2_inner < log2ct &&
+      lj.log2_n + lj.log2_inner <= 8) {
+    int const log2blk = lj.log2_n + lj.log2_inner;
+    dims[0] = static_cast<cuuint64_t>(1) << log2blk;
+    dims[1] = 1;
+    strides[0] = static_cast<cuuint64_t>(4) << log2blk;
+    box[0] = 1u << log2blk;
+    box[1] = 1;
+  }
   cuuint32_t elem[3] = {1, 1, 1};
   CUresult const res = encode(
       &map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
